@@ -1,0 +1,738 @@
+// C-ABI entry points of rg300 (include/rg300.h), the host-side preparation of
+// the device data structures (CRS layout, element->CRS slot map, element
+// colouring, ILU(0) schedule) and the Newton-correction kernels.
+
+#include "rg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+rg_status rg_fail(rg_ctx* c, rg_status s, const char* msg) {
+  if (c) c->err = msg ? msg : "";
+  return s;
+}
+
+rg_status rg_cuda(rg_ctx* c, cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return RG_OK;
+  if (c) {
+    c->err = std::string(where) + ": " + cudaGetErrorString(e);
+  }
+  return RG_ERR_CUDA;
+}
+
+#define TRY(expr)                                        \
+  do {                                                   \
+    cudaError_t _e = (expr);                             \
+    if (_e != cudaSuccess) return rg_cuda(c, _e, #expr); \
+  } while (0)
+
+template <class T>
+static cudaError_t upload(rg_ctx* c, DBuf<T>& d, const T* h, size_t n) {
+  cudaError_t e = d.alloc(n);
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->st);
+}
+
+template <class T>
+static cudaError_t upload_if(rg_ctx* c, DBuf<T>& d, const T* h, size_t n) {
+  if (!h) return cudaSuccess;
+  if (d.n != n) {
+    cudaError_t e = d.alloc(n);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->st);
+}
+
+static rg_status check_device_error(rg_ctx* c) {
+  TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  int e = *c->err_host;
+  if (e == 0) return RG_OK;
+  TRY(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), c->st));
+  if (e & 2) return rg_fail(c, RG_ERR_ZERO_PIVOT, "ILU(0) zero pivot without a repair row");
+  if (e & 4) return rg_fail(c, RG_ERR_ARG, "CRS row wider than the supported maximum");
+  return rg_fail(c, RG_ERR_DEVICE_WAIT, "a bounded device-side wait ran out");
+}
+
+// =============================================================================
+// Newton correction kernels (EqsUVS2D.cpp:455-759, Update.cpp:42-187)
+
+namespace {
+
+__device__ __forceinline__ double atomic_max_pos(double* addr, double v) {
+  // non-negative doubles order like their bit patterns
+  return __longlong_as_double(atomicMax((long long*)addr, __double_as_longlong(v)));
+}
+
+// upd[0..2] max|X| per variable, [3] sum of squares, [4] max |dUs|, [5] max |dS|
+__global__ void k_upd_reduce(int npm, const int* __restrict__ mnodes, const int* __restrict__ eqno,
+                             const double* __restrict__ X, double* upd) {
+  double m0 = 0, m1 = 0, m2 = 0, ss = 0, mus = 0, ms = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npm; t += gridDim.x * blockDim.x) {
+    const int n = mnodes[t];
+    const int qU = eqno[3 * n], qV = eqno[3 * n + 1], qS = eqno[3 * n + 2];
+    double dU = qU >= 0 ? fabs(X[qU]) : 0.0;
+    double dV = qV >= 0 ? fabs(X[qV]) : 0.0;
+    double dS = qS >= 0 ? fabs(X[qS]) : 0.0;
+    m0 = fmax(m0, dU);
+    m1 = fmax(m1, dV);
+    m2 = fmax(m2, dS);
+    ss += dU * dU + dV * dV + dS * dS;
+    mus = fmax(mus, sqrt(dU * dU + dV * dV));
+    ms = fmax(ms, dS);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m0 = fmax(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    mus = fmax(mus, __shfl_xor_sync(0xffffffffu, mus, o));
+    ms = fmax(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_pos(&upd[0], m0);
+    atomic_max_pos(&upd[1], m1);
+    atomic_max_pos(&upd[2], m2);
+    atomicAdd(&upd[3], ss);   // reported only (relaxation "norm"); order-dependent in the last bits
+    atomic_max_pos(&upd[4], mus);
+    atomic_max_pos(&upd[5], ms);
+  }
+}
+
+// relaxation factors (method 0 / 2, EqsUVS2D.cpp:461-544)
+__global__ void k_upd_relax(double* upd, int method, double maxDeltaUV, double maxDeltaS) {
+  double relaxUs = 1.0, relaxS = 1.0;
+  if (method == 2) {
+    relaxUs = maxDeltaUV / upd[4];
+    relaxS = maxDeltaS / upd[5];
+    if (relaxUs > 1.0) relaxUs = 1.0;
+    if (relaxS > 1.0) relaxS = 1.0;
+  }
+  upd[6] = relaxUs;
+  upd[7] = relaxS;
+  upd[8] = sqrt(upd[3]);
+}
+
+__global__ void k_upd_apply(int npm, const int* __restrict__ mnodes, const int* __restrict__ eqno,
+                            const int* __restrict__ nflag, const double* __restrict__ rot,
+                            const double* __restrict__ X, const double* upd, double* U, double* V, double* S,
+                            double* z, const double* __restrict__ zor, double maxUs, double dryLimit, int drymethod,
+                            double hmin) {
+  const double relaxUs = upd[6], relaxS = upd[7];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npm; t += gridDim.x * blockDim.x) {
+    const int n = mnodes[t];
+    const int qU = eqno[3 * n], qV = eqno[3 * n + 1], qS = eqno[3 * n + 2];
+    double dU = qU >= 0 ? X[qU] * relaxUs : 0.0;
+    double dV = qV >= 0 ? X[qV] * relaxUs : 0.0;
+    double dS = qS >= 0 ? X[qS] * relaxS : 0.0;
+    double u = U[n], v = V[n];
+    if (nflag[n] & RG_N_ROTAT) {
+      const double* r = rot + 4 * n;
+      u += r[0] * dU;
+      v += r[2] * dU;
+      u += r[1] * dV;
+      v += r[3] * dV;
+    } else {
+      u += dU;
+      v += dV;
+    }
+    const double Us = sqrt(u * u + v * v);
+    if (Us > maxUs) {
+      u = u * maxUs / Us;
+      v = v * maxUs / Us;
+    }
+    U[n] = u;
+    V[n] = v;
+    if (qS >= 0) {
+      double s = S[n] + dS;
+      if (drymethod == 0 || drymethod == 2 || drymethod == 3) {
+        const double H = s - zor[n];
+        z[n] = (H < dryLimit) ? s - dryLimit : zor[n];
+      } else {
+        if (s - z[n] <= 0.0) s = z[n] + hmin;
+      }
+      S[n] = s;
+    }
+  }
+}
+
+// mid-side S and z as corner means over all region triangles (EqsUVS2D.cpp:735-759)
+__global__ void k_upd_midside(int ner, const int* __restrict__ rnodes, double* S, double* z) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ner; e += gridDim.x * blockDim.x) {
+    const int* nd = rnodes + 6 * e;
+    if (nd[3] < 0) continue;
+#pragma unroll
+    for (int i = 3; i < 6; i++) {
+      const int l = nd[i - 3], r = nd[(i - 2) % 3];
+      S[nd[i]] = 0.5 * (S[l] + S[r]);
+      z[nd[i]] = 0.5 * (z[l] + z[r]);
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_update(rg_ctx* c, const rg_update_opts* o, double* stats) {
+  cudaError_t e = cudaMemsetAsync(c->upd.p, 0, 16 * sizeof(double), c->st);
+  if (e != cudaSuccess) return e;
+  int nb = (c->np_model + 255) / 256;
+  if (nb > c->num_sms * 8) nb = c->num_sms * 8;
+  if (nb < 1) nb = 1;
+  k_upd_reduce<<<nb, 256, 0, c->st>>>(c->np_model, c->model_nodes.p, c->eqno.p, c->X.p, c->upd.p);
+  k_upd_relax<<<1, 1, 0, c->st>>>(c->upd.p, o->relax_method, o->max_delta_uv, o->max_delta_s);
+  k_upd_apply<<<nb, 256, 0, c->st>>>(c->np_model, c->model_nodes.p, c->eqno.p, c->nflag.p, c->rot.p, c->X.p,
+                                     c->upd.p, c->U.p, c->V.p, c->S.p, c->z.p, c->zor.p, o->max_us, o->dry_limit,
+                                     o->dryrew_method, c->hmin);
+  int nbe = (c->ne_region + 255) / 256;
+  if (nbe < 1) nbe = 1;
+  k_upd_midside<<<nbe, 256, 0, c->st>>>(c->ne_region, c->region_nodes.p, c->S.p, c->z.p);
+  double h[16];
+  e = cudaMemcpyAsync(h, c->upd.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return e;
+  if (stats) {
+    stats[0] = h[0];
+    stats[1] = h[1];
+    stats[2] = h[2];
+    stats[3] = h[6];
+    stats[4] = h[7];
+    stats[5] = h[8];
+  }
+  return cudaGetLastError();
+}
+
+// =============================================================================
+// C ABI
+
+extern "C" {
+
+const char* rg_version(void) { return "rg300 0.1 (sm_103a)"; }
+
+const char* rg_last_error(rg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+rg_status rg_create(const rg_mesh* m, int precision, int device, rg_ctx** out) {
+  if (!m || !out || m->np <= 0 || m->ne < 0 || !m->x || !m->y || !m->elem_nodes || !m->elem_nnd ||
+      !m->elem_flag || !m->elem_vt)
+    return RG_ERR_ARG;
+  if (precision < RG_PREC_FP64 || precision > RG_PREC_MIXED) return RG_ERR_ARG;
+  for (int e = 0; e < m->ne; e++) {
+    int nnd = m->elem_nnd[e];
+    if (nnd != 6 && nnd != 3) return RG_ERR_ARG;
+    for (int i = 0; i < nnd; i++) {
+      int k = m->elem_nodes[6 * e + i];
+      if (k < 0 || k >= m->np) return RG_ERR_ARG;
+    }
+  }
+  rg_ctx* c = new rg_ctx();
+  *out = c;
+  c->prec = precision;
+  if (device < 0) {
+    TRY(cudaGetDevice(&c->device));
+  } else {
+    c->device = device;
+  }
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+  int coop = 0;
+  TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
+  if (!coop) return rg_fail(c, RG_ERR_CUDA, "device does not support cooperative launches");
+  TRY(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  for (int i = 0; i < 16; i++) TRY(cudaEventCreate(&c->ev[i]));
+  TRY(cudaMallocHost((void**)&c->ks_host, sizeof(KrylovScalars)));
+  TRY(cudaMallocHost((void**)&c->err_host, sizeof(int)));
+  c->np = m->np;
+  c->ne = m->ne;
+  c->g = m->g;
+  c->hmin = m->hmin;
+  c->vk = m->vk;
+  TRY(upload(c, c->x, m->x, m->np));
+  TRY(upload(c, c->y, m->y, m->np));
+  TRY(upload(c, c->enodes, m->elem_nodes, 6 * (size_t)m->ne));
+  TRY(upload(c, c->ennd, m->elem_nnd, m->ne));
+  TRY(upload(c, c->eflag, m->elem_flag, m->ne));
+  TRY(upload(c, c->evt, m->elem_vt, m->ne));
+  // keep host copies needed by the pattern preparation
+  c->h_enodes.assign(m->elem_nodes, m->elem_nodes + 6 * (size_t)m->ne);
+  c->h_ennd.assign(m->elem_nnd, m->elem_nnd + m->ne);
+  c->h_eflag.assign(m->elem_flag, m->elem_flag + m->ne);
+  const size_t np = m->np;
+  for (DBuf<double>* b : {&c->U, &c->V, &c->S, &c->dUdt, &c->dVdt, &c->dSdt, &c->z, &c->cf, &c->cfw, &c->niox,
+                          &c->nioy, &c->bcU, &c->bcS}) {
+    TRY(b->alloc(np));
+    TRY(cudaMemsetAsync(b->p, 0, np * sizeof(double), c->st));
+  }
+  TRY(c->rot.alloc(4 * np));
+  TRY(cudaMemsetAsync(c->rot.p, 0, 4 * np * sizeof(double), c->st));
+  TRY(c->nflag.alloc(np));
+  TRY(c->bckind.alloc(np));
+  TRY(cudaMemsetAsync(c->nflag.p, 0, np * sizeof(int), c->st));
+  TRY(cudaMemsetAsync(c->bckind.p, 0, np * sizeof(int), c->st));
+  TRY(c->ks.alloc(1));
+  TRY(cudaMemsetAsync(c->ks.p, 0, sizeof(KrylovScalars), c->st));
+  TRY(c->dev_err.alloc(1));
+  TRY(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), c->st));
+  TRY(c->upd.alloc(16));
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_destroy(rg_ctx* c) {
+  if (!c) return RG_OK;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->ks_host) cudaFreeHost(c->ks_host);
+  if (c->err_host) cudaFreeHost(c->err_host);
+  for (int i = 0; i < 16; i++)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return RG_OK;
+}
+
+rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index, const int* eqno) {
+  if (!c || neq <= 0 || !width || !index || !eqno) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: bad arguments");
+  TRY(cudaSetDevice(c->device));
+  // CRS layout
+  std::vector<int> rowptr(neq + 1, 0);
+  for (int i = 0; i < neq; i++) {
+    if (width[i] < 1 || width[i] > RG_MAXW) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: row width out of range");
+    rowptr[i + 1] = rowptr[i] + width[i];
+  }
+  const int nnz = rowptr[neq];
+  for (int i = 0; i < neq; i++) {
+    if (index[rowptr[i]] != i) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: diagonal must come first");
+    for (int q = rowptr[i]; q < rowptr[i + 1]; q++)
+      if (index[q] < 0 || index[q] >= neq) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: column out of range");
+  }
+  for (int k = 0; k < 3 * c->np; k++)
+    if (eqno[k] < -1 || eqno[k] >= neq) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: bad equation number");
+  c->neq = neq;
+  c->nnz = nnz;
+  c->h_rowptr = rowptr;
+  c->h_col.assign(index, index + nnz);
+  TRY(upload(c, c->rowptr, rowptr.data(), rowptr.size()));
+  TRY(upload(c, c->col, index, (size_t)nnz));
+  TRY(upload(c, c->eqno, eqno, 3 * (size_t)c->np));
+
+  // element rows and slot map (the linear searches of Assemble.cpp:256-263,
+  // done once per pattern instead of once per entry and iteration)
+  const int ne = c->ne;
+  std::vector<int> erow((size_t)ne * RG_EQ, -1), slot((size_t)ne * RG_EQ * RG_EQ, -1);
+  for (int e = 0; e < ne; e++) {
+    const int nnd = c->h_ennd[e];
+    const int* nd = &c->h_enodes[6 * (size_t)e];
+    int eq[RG_EQ];
+    for (int r = 0; r < RG_EQ; r++) eq[r] = -1;
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < nnd; i++) {
+        int r = i + j * nnd;
+        if (r < RG_EQ) eq[r] = eqno[3 * nd[i] + j];
+      }
+    for (int r = 0; r < RG_EQ; r++) {
+      erow[(size_t)e * RG_EQ + r] = eq[r];
+      if (eq[r] < 0) continue;
+      for (int cc = 0; cc < RG_EQ; cc++) {
+        if (eq[cc] < 0) continue;
+        for (int q = rowptr[eq[r]]; q < rowptr[eq[r] + 1]; q++)
+          if (index[q] == eq[cc]) {
+            slot[((size_t)e * RG_EQ + r) * RG_EQ + cc] = q;
+            break;
+          }
+      }
+    }
+  }
+  TRY(upload(c, c->erow, erow.data(), erow.size()));
+  TRY(upload(c, c->slot, slot.data(), slot.size()));
+
+  // greedy colouring: no two elements of a colour share a node, so their
+  // scatters touch disjoint CRS rows
+  std::vector<unsigned long long> used(c->np, 0ull);
+  std::vector<int> color(ne, -1);
+  int ncol = 0;
+  for (int e = 0; e < ne; e++) {
+    if (c->h_eflag[e] & RG_E_DRY) continue;   // EQS_UVS2D::Coefs skips dry elements
+    const int nnd = c->h_ennd[e];
+    const int* nd = &c->h_enodes[6 * (size_t)e];
+    unsigned long long forb = 0;
+    for (int i = 0; i < nnd; i++) forb |= used[nd[i]];
+    int k = 0;
+    while (k < 64 && (forb >> k) & 1ull) k++;
+    if (k >= 64) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: more than 64 element colours needed");
+    color[e] = k;
+    for (int i = 0; i < nnd; i++) used[nd[i]] |= 1ull << k;
+    ncol = std::max(ncol, k + 1);
+  }
+  std::vector<int> celem;
+  c->color_ptr.assign(3 * (size_t)ncol, 0);
+  for (int k = 0; k < ncol; k++) {
+    c->color_ptr[3 * k] = (int)celem.size();
+    for (int e = 0; e < ne; e++)
+      if (color[e] == k && !(c->h_eflag[e] & RG_E_BOUND)) celem.push_back(e);
+    c->color_ptr[3 * k + 1] = (int)celem.size();
+    for (int e = 0; e < ne; e++)
+      if (color[e] == k && (c->h_eflag[e] & RG_E_BOUND)) celem.push_back(e);
+    c->color_ptr[3 * k + 2] = (int)celem.size();
+  }
+  TRY(upload(c, c->color_elem, celem.data(), celem.size()));
+
+  // ILU(0) schedule: L positions sorted by column; split L/U operands
+  std::vector<int> lsp(neq + 1, 0), lspos, Lptr(neq + 1, 0), Lcol, Lsrc, Uptr(neq + 1, 0), Ucol, Usrc;
+  std::vector<std::pair<int, int>> tmp;
+  for (int i = 0; i < neq; i++) {
+    tmp.clear();
+    for (int q = rowptr[i] + 1; q < rowptr[i + 1]; q++) {
+      if (index[q] < i) {
+        tmp.push_back({index[q], q - rowptr[i]});
+        Lcol.push_back(index[q]);
+        Lsrc.push_back(q);
+      } else if (index[q] > i) {
+        Ucol.push_back(index[q]);
+        Usrc.push_back(q);
+      }
+    }
+    std::sort(tmp.begin(), tmp.end());
+    for (auto& p : tmp) lspos.push_back(p.second);
+    lsp[i + 1] = (int)lspos.size();
+    Lptr[i + 1] = (int)Lcol.size();
+    Uptr[i + 1] = (int)Ucol.size();
+  }
+  TRY(upload(c, c->lsort_ptr, lsp.data(), lsp.size()));
+  TRY(upload(c, c->lsort_pos, lspos.data(), std::max<size_t>(lspos.size(), 1)));
+  TRY(upload(c, c->Lptr, Lptr.data(), Lptr.size()));
+  TRY(upload(c, c->Lcol, Lcol.data(), Lcol.size()));
+  TRY(upload(c, c->Lsrc, Lsrc.data(), Lsrc.size()));
+  TRY(upload(c, c->Uptr, Uptr.data(), Uptr.size()));
+  TRY(upload(c, c->Ucol, Ucol.data(), Ucol.size()));
+  TRY(upload(c, c->Usrc, Usrc.data(), Usrc.size()));
+  TRY(c->fflag.alloc(neq));
+  TRY(cudaMemsetAsync(c->fflag.p, 0, neq * sizeof(int), c->st));
+  c->fepoch = 0;
+
+  // values and work vectors
+  const size_t n = neq;
+  if (c->prec == RG_PREC_FP64) {
+    TRY(c->A64.alloc(nnz));
+    TRY(c->LU64.alloc(nnz));
+    TRY(c->Lv64.alloc(std::max<size_t>(Lcol.size(), 1)));
+    TRY(c->Uv64.alloc(std::max<size_t>(Ucol.size(), 1)));
+    TRY(c->Dv64.alloc(n));
+  } else {
+    TRY(c->A32.alloc(nnz));
+    TRY(c->LU32.alloc(nnz));
+    TRY(c->Lv32.alloc(std::max<size_t>(Lcol.size(), 1)));
+    TRY(c->Uv32.alloc(std::max<size_t>(Ucol.size(), 1)));
+    TRY(c->Dv32.alloc(n));
+  }
+  TRY(c->B.alloc(n));
+  for (DBuf<double>* b : {&c->r0, &c->ri, &c->vi, &c->pi, &c->yi, &c->zi, &c->ti, &c->tt, &c->xm, &c->X, &c->tmp})
+    TRY(b->alloc(n));
+  if (c->prec == RG_PREC_MIXED)
+    for (DBuf<float>* b : {&c->f_r0, &c->f_ri, &c->f_vi, &c->f_pi, &c->f_yi, &c->f_zi, &c->f_ti, &c->f_x, &c->f_xm,
+                           &c->f_b, &c->f_w})
+      TRY(b->alloc(n));
+  TRY(c->partial.alloc((size_t)c->num_sms * 8 * 4 + 64));
+  c->have_system = false;
+  c->have_factor = false;
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_set_boundary(rg_ctx* c, const int* nflag, const int* bckind, const double* rot, const double* niox,
+                          const double* nioy, const double* bcU, const double* bcS) {
+  if (!c) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  const size_t np = c->np;
+  TRY(upload_if(c, c->nflag, nflag, np));
+  TRY(upload_if(c, c->bckind, bckind, np));
+  TRY(upload_if(c, c->rot, rot, 4 * np));
+  TRY(upload_if(c, c->niox, niox, np));
+  TRY(upload_if(c, c->nioy, nioy, np));
+  TRY(upload_if(c, c->bcU, bcU, np));
+  TRY(upload_if(c, c->bcS, bcS, np));
+  c->have_boundary = true;
+  return RG_OK;
+}
+
+rg_status rg_set_state(rg_ctx* c, const double* U, const double* V, const double* S, const double* dUdt,
+                       const double* dVdt, const double* dSdt, const double* z, const double* cf, const double* cfw) {
+  if (!c) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  const size_t np = c->np;
+  TRY(upload_if(c, c->U, U, np));
+  TRY(upload_if(c, c->V, V, np));
+  TRY(upload_if(c, c->S, S, np));
+  TRY(upload_if(c, c->dUdt, dUdt, np));
+  TRY(upload_if(c, c->dVdt, dVdt, np));
+  TRY(upload_if(c, c->dSdt, dSdt, np));
+  TRY(upload_if(c, c->z, z, np));
+  TRY(upload_if(c, c->cf, cf, np));
+  TRY(upload_if(c, c->cfw, cfw, np));
+  return RG_OK;
+}
+
+rg_status rg_get_state(rg_ctx* c, double* U, double* V, double* S, double* z) {
+  if (!c) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  const size_t b = c->np * sizeof(double);
+  if (U) TRY(cudaMemcpyAsync(U, c->U.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (V) TRY(cudaMemcpyAsync(V, c->V.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (S) TRY(cudaMemcpyAsync(S, c->S.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (z) TRY(cudaMemcpyAsync(z, c->z.p, b, cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_set_relax(rg_ctx* c, double relaxThdt_UV, double relaxThdt_H) {
+  if (!c) return RG_ERR_ARG;
+  c->rUV = relaxThdt_UV;
+  c->rH = relaxThdt_H;
+  return RG_OK;
+}
+
+static rg_status copy_out_system(rg_ctx* c, double* B_out, float* A32_out, double* A64_out, bool lu) {
+  if (B_out) TRY(cudaMemcpyAsync(B_out, c->B.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (c->prec == RG_PREC_FP64) {
+    const double* src = lu ? c->LU64.p : c->A64.p;
+    if (A64_out) TRY(cudaMemcpyAsync(A64_out, src, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    if (A32_out) {
+      std::vector<double> tmp(c->nnz);
+      TRY(cudaMemcpyAsync(tmp.data(), src, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      TRY(cudaStreamSynchronize(c->st));
+      for (int64_t i = 0; i < c->nnz; i++) A32_out[i] = (float)tmp[i];
+    }
+  } else {
+    const float* src = lu ? c->LU32.p : c->A32.p;
+    if (A32_out) TRY(cudaMemcpyAsync(A32_out, src, c->nnz * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    if (A64_out) {
+      std::vector<float> tmp(c->nnz);
+      TRY(cudaMemcpyAsync(tmp.data(), src, c->nnz * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+      TRY(cudaStreamSynchronize(c->st));
+      for (int64_t i = 0; i < c->nnz; i++) A64_out[i] = (double)tmp[i];
+    }
+  }
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_assemble(rg_ctx* c, double* B_out, float* A32_out, double* A64_out) {
+  if (!c || c->neq <= 0) return rg_fail(c, RG_ERR_ARG, "rg_assemble: no pattern");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaEventRecord(c->ev[0], c->st));
+  TRY(launch_assemble(c));
+  TRY(cudaEventRecord(c->ev[1], c->st));
+  TRY(cudaEventSynchronize(c->ev[1]));
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+  c->t_ms[0] = ms;
+  c->have_system = true;
+  c->have_factor = false;
+  return copy_out_system(c, B_out, A32_out, A64_out, false);
+}
+
+rg_status rg_load_system(rg_ctx* c, const float* A32, const double* A64, const double* B) {
+  if (!c || c->neq <= 0 || (!A32 == !A64) || !B) return rg_fail(c, RG_ERR_ARG, "rg_load_system: bad arguments");
+  TRY(cudaSetDevice(c->device));
+  if (c->prec == RG_PREC_FP64) {
+    if (A64) {
+      TRY(cudaMemcpyAsync(c->A64.p, A64, c->nnz * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    } else {
+      std::vector<double> t(A32, A32 + c->nnz);
+      TRY(cudaMemcpyAsync(c->A64.p, t.data(), c->nnz * sizeof(double), cudaMemcpyHostToDevice, c->st));
+      TRY(cudaStreamSynchronize(c->st));
+    }
+  } else {
+    if (A32) {
+      TRY(cudaMemcpyAsync(c->A32.p, A32, c->nnz * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    } else {
+      std::vector<float> t(c->nnz);
+      for (int64_t i = 0; i < c->nnz; i++) t[i] = (float)A64[i];
+      TRY(cudaMemcpyAsync(c->A32.p, t.data(), c->nnz * sizeof(float), cudaMemcpyHostToDevice, c->st));
+      TRY(cudaStreamSynchronize(c->st));
+    }
+  }
+  TRY(cudaMemcpyAsync(c->B.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  c->have_system = true;
+  c->have_factor = false;
+  return RG_OK;
+}
+
+rg_status rg_scale(rg_ctx* c, double* scale) {
+  if (!c || !c->have_system) return rg_fail(c, RG_ERR_ARG, "rg_scale: no system");
+  TRY(cudaSetDevice(c->device));
+  double s = 0;
+  TRY(cudaEventRecord(c->ev[2], c->st));
+  TRY(launch_scale(c, &s));
+  TRY(cudaEventRecord(c->ev[3], c->st));
+  TRY(cudaEventSynchronize(c->ev[3]));
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+  c->t_ms[1] = ms;
+  if (scale) *scale = s;
+  if (!(s == s)) return rg_fail(c, RG_ERR_NONFINITE, "rg_scale: non-finite residual norm");
+  return RG_OK;
+}
+
+rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
+  if (!c || !c->have_system) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_factor: no system");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaEventRecord(c->ev[4], c->st));
+  TRY(launch_factor(c));
+  TRY(launch_split(c));
+  TRY(cudaEventRecord(c->ev[5], c->st));
+  rg_status s = check_device_error(c);
+  if (s != RG_OK) return s;
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]));
+  c->t_ms[2] = ms;
+  c->have_factor = true;
+  if (LU32_out || LU64_out) return copy_out_system(c, nullptr, LU32_out, LU64_out, true);
+  return RG_OK;
+}
+
+rg_status rg_ilu0_apply(rg_ctx* c, const double* B, double* X) {
+  if (!c || !c->have_factor || !B || !X) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply: no factors");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaMemcpyAsync(c->ri.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  TRY(cudaEventRecord(c->ev[6], c->st));
+  TRY(launch_ilu_apply_d(c, c->ri.p, c->zi.p));
+  TRY(cudaEventRecord(c->ev[7], c->st));
+  rg_status s = check_device_error(c);
+  if (s != RG_OK) return s;
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
+  c->t_ms[5] = ms;
+  TRY(cudaMemcpyAsync(X, c->zi.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_spmv(rg_ctx* c, const double* x, double* r) {
+  if (!c || !c->have_system || !x || !r) return rg_fail(c, RG_ERR_ARG, "rg_spmv: no system");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaMemcpyAsync(c->pi.p, x, c->neq * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  TRY(cudaEventRecord(c->ev[8], c->st));
+  TRY(launch_spmv_d(c, c->pi.p, c->vi.p));
+  TRY(cudaEventRecord(c->ev[9], c->st));
+  TRY(cudaMemcpyAsync(r, c->vi.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[8], c->ev[9]));
+  c->t_ms[4] = ms;
+  return RG_OK;
+}
+
+rg_status rg_bicgstab(rg_ctx* c, int maxIter, double maxDiff, double* X_out, int* iters, double* accuracy) {
+  if (!c || !c->have_factor || maxIter <= 0) return rg_fail(c, RG_ERR_ARG, "rg_bicgstab: no factors");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaEventRecord(c->ev[10], c->st));
+  rg_status s = run_bicgstab(c, maxIter, maxDiff, iters, accuracy);
+  TRY(cudaEventRecord(c->ev[11], c->st));
+  rg_status d = check_device_error(c);
+  if (d != RG_OK) return d;
+  if (s != RG_OK && s != RG_NOT_CONVERGED) return s;
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[10], c->ev[11]));
+  c->t_ms[3] = ms;
+  if (X_out) {
+    TRY(cudaMemcpyAsync(X_out, c->X.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    TRY(cudaStreamSynchronize(c->st));
+  }
+  return s;
+}
+
+rg_status rg_solve(rg_ctx* c, int maxIter, double maxDiff, double* X_out, double* scale_out, int* iters_out) {
+  if (!c || c->neq <= 0 || !c->have_boundary) return rg_fail(c, RG_ERR_ARG, "rg_solve: pattern/boundary missing");
+  rg_status s = rg_assemble(c, nullptr, nullptr, nullptr);
+  if (s != RG_OK) return s;
+  s = rg_scale(c, scale_out);
+  if (s != RG_OK) return s;
+  s = rg_ilu0_factor(c, nullptr, nullptr);
+  if (s != RG_OK) return s;
+  return rg_bicgstab(c, maxIter, maxDiff, X_out, iters_out, nullptr);
+}
+
+rg_status rg_set_update_lists(rg_ctx* c, int np_model, const int* model_nodes, int ne_region,
+                              const int* region_nodes, const double* zor) {
+  if (!c || np_model < 0 || ne_region < 0 || (np_model && !model_nodes) || (ne_region && !region_nodes) || !zor)
+    return rg_fail(c, RG_ERR_ARG, "rg_set_update_lists: bad arguments");
+  TRY(cudaSetDevice(c->device));
+  for (int i = 0; i < np_model; i++)
+    if (model_nodes[i] < 0 || model_nodes[i] >= c->np) return rg_fail(c, RG_ERR_ARG, "bad model node");
+  for (int i = 0; i < 6 * ne_region; i++)
+    if (region_nodes[i] < -1 || region_nodes[i] >= c->np) return rg_fail(c, RG_ERR_ARG, "bad region node");
+  c->np_model = np_model;
+  c->ne_region = ne_region;
+  TRY(upload(c, c->model_nodes, model_nodes, std::max(np_model, 1)));
+  TRY(upload(c, c->region_nodes, region_nodes, 6 * (size_t)std::max(ne_region, 1)));
+  TRY(upload(c, c->zor, zor, c->np));
+  c->h_region_nodes.assign(region_nodes, region_nodes + 6 * (size_t)ne_region);
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_newton_update(rg_ctx* c, const rg_update_opts* o, double* stats) {
+  if (!c || !o || c->neq <= 0 || !c->model_nodes.p) return rg_fail(c, RG_ERR_ARG, "rg_newton_update: not set up");
+  if (o->relax_method != 0 && o->relax_method != 2)
+    return rg_fail(c, RG_ERR_ARG, "rg_newton_update: relaxation method must be 0 or 2");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaEventRecord(c->ev[12], c->st));
+  TRY(launch_update(c, o, stats));
+  TRY(cudaEventRecord(c->ev[13], c->st));
+  TRY(cudaEventSynchronize(c->ev[13]));
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[12], c->ev[13]));
+  c->t_ms[6] = ms;
+  return RG_OK;
+}
+
+rg_status rg_set_friction(rg_ctx* c, const double* elem_n, const double* elem_areafact) {
+  if (!c || !elem_n || !elem_areafact || c->h_region_nodes.empty())
+    return rg_fail(c, RG_ERR_ARG, "rg_set_friction: call rg_set_update_lists first");
+  TRY(cudaSetDevice(c->device));
+  const int ner = c->ne_region;
+  std::vector<int> cnt(c->np + 1, 0);
+  for (int e = 0; e < ner; e++)
+    for (int i = 0; i < 6; i++) {
+      int k = c->h_region_nodes[6 * (size_t)e + i];
+      if (k >= 0) cnt[k + 1]++;
+    }
+  for (int k = 0; k < c->np; k++) cnt[k + 1] += cnt[k];
+  std::vector<int> el(cnt[c->np]), pos(cnt.begin(), cnt.end() - 1);
+  for (int e = 0; e < ner; e++)
+    for (int i = 0; i < 6; i++) {
+      int k = c->h_region_nodes[6 * (size_t)e + i];
+      if (k >= 0) el[pos[k]++] = e;
+    }
+  TRY(upload(c, c->fr_ptr, cnt.data(), cnt.size()));
+  TRY(upload(c, c->fr_el, el.data(), std::max<size_t>(el.size(), 1)));
+  TRY(upload(c, c->elem_n, elem_n, std::max(ner, 1)));
+  TRY(upload(c, c->elem_af, elem_areafact, std::max(ner, 1)));
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_friction(rg_ctx* c, double* cf_out) {
+  if (!c || !c->fr_ptr.p) return rg_fail(c, RG_ERR_ARG, "rg_friction: call rg_set_friction first");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaEventRecord(c->ev[14], c->st));
+  TRY(launch_friction(c));
+  TRY(cudaEventRecord(c->ev[15], c->st));
+  if (cf_out) TRY(cudaMemcpyAsync(cf_out, c->cf.p, c->np * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  float ms = 0;
+  TRY(cudaEventElapsedTime(&ms, c->ev[14], c->ev[15]));
+  c->t_ms[7] = ms;
+  return RG_OK;
+}
+
+rg_status rg_get_timings(rg_ctx* c, double* ms, int n) {
+  if (!c || !ms) return RG_ERR_ARG;
+  for (int i = 0; i < n && i < 8; i++) ms[i] = c->t_ms[i];
+  return RG_OK;
+}
+
+}  // extern "C"

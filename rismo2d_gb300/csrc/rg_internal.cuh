@@ -1,0 +1,147 @@
+// Internal declarations of the rg300 library (not part of the C ABI).
+#pragma once
+
+#include "../../include/rg300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+// widest CRS row the warp kernels handle (the reference's default mceq is 100,
+// Project.cpp:1706-1752; P2 triangles give at most ~45)
+#define RG_MAXW 128
+
+// element-matrix size: 3 dof x 5 rows used by a P2 triangle (15), stored 16 wide
+#define RG_EQ 15
+#define RG_KSTRIDE 16
+
+// reference flag bits (Node.h, Elem.h, Bcon.h)
+#define RG_N_ROTAT    32
+#define RG_E_INLET     1
+#define RG_E_OUTLET    2
+#define RG_E_OPENBND   4
+#define RG_E_BOUND    16
+#define RG_E_DRY     128
+#define RG_B_INLET     1
+#define RG_B_OUTLET    2
+#define RG_B_OPENBND   4
+#define RG_B_LOGLAW  256
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  cudaError_t alloc(size_t count) {
+    if (count == n && p) return cudaSuccess;
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// per-solve scalars kept on the device (BiCGStab state, reductions)
+struct KrylovScalars {
+  double rho, alfa, omega, beta;
+  double l2r0, diff, accuracy;
+  double t1, t2;
+  int it, done, conv, restarts;
+};
+
+struct rg_ctx {
+  int device = 0;
+  int prec = RG_PREC_FP64;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int num_sms = 0;
+
+  // mesh and constants
+  int np = 0, ne = 0;
+  double g = 9.81, hmin = 0.0, vk = 0.0, rUV = 0.0, rH = 0.0;
+  DBuf<double> x, y, evt;
+  DBuf<int> enodes, ennd, eflag;
+  std::vector<int> h_enodes, h_ennd, h_eflag, h_region_nodes;
+
+  // node state and boundary data
+  DBuf<double> U, V, S, dUdt, dVdt, dSdt, z, cf, cfw;
+  DBuf<int> nflag, bckind;
+  DBuf<double> rot, niox, nioy, bcU, bcS;
+  bool have_boundary = false;
+
+  // pattern (reference layout: diagonal first, first-seen column order)
+  int neq = 0;
+  int64_t nnz = 0;
+  std::vector<int> h_rowptr, h_col;
+  DBuf<int> eqno, rowptr, col;
+  DBuf<int> slot;            // per element RG_EQ*RG_EQ CRS positions (-1 = none)
+  DBuf<int> erow;            // per element RG_EQ equation numbers of its rows
+  std::vector<int> color_ptr;
+  DBuf<int> color_elem;      // elements grouped by colour
+
+  // values
+  DBuf<double> A64, LU64;
+  DBuf<float> A32, LU32;
+  DBuf<double> B;
+  bool have_system = false, have_factor = false;
+
+  // ILU(0) factor schedule: per row, L positions sorted by column
+  DBuf<int> lsort_ptr, lsort_pos;
+  DBuf<int> fflag;           // row-done flags of the factorisation (epoch valued)
+  int fepoch = 0;
+
+  // triangular-solve operands split from the factors
+  DBuf<int> Lptr, Lcol, Lsrc, Uptr, Ucol, Usrc;
+  DBuf<double> Lv64, Uv64, Dv64;
+  DBuf<float> Lv32, Uv32, Dv32;
+
+  // Krylov vectors (double) and float copies for the mixed path
+  DBuf<double> r0, ri, vi, pi, yi, zi, ti, tt, xm, X, tmp;
+  DBuf<float> f_r0, f_ri, f_vi, f_pi, f_yi, f_zi, f_ti, f_x, f_xm, f_b, f_w;
+  DBuf<double> partial;      // block partial sums of reductions
+  DBuf<KrylovScalars> ks;
+  KrylovScalars* ks_host = nullptr;   // pinned mirror
+  DBuf<int> dev_err;         // device error word
+  int* err_host = nullptr;
+
+  // Newton update
+  DBuf<int> model_nodes, region_nodes;
+  DBuf<double> zor, upd;     // upd: reduction scratch
+  int np_model = 0, ne_region = 0;
+  DBuf<double> elem_n, elem_af;  // friction: Manning n, area factor per region triangle
+  DBuf<int> fr_ptr, fr_el;       // node -> region triangles (element order)
+
+  // timings
+  cudaEvent_t ev[16];
+  double t_ms[8] = {0};
+
+  int persist_blocks = 0;    // co-resident blocks for the persistent kernels
+};
+
+// ---- launchers implemented in the .cu files -------------------------------
+rg_status rg_fail(rg_ctx* c, rg_status s, const char* msg);
+rg_status rg_cuda(rg_ctx* c, cudaError_t e, const char* where);
+
+// assembly (rg_assemble.cu)
+cudaError_t launch_assemble(rg_ctx* c);
+cudaError_t launch_friction(rg_ctx* c);
+
+// linear algebra (rg_linalg.cu)
+cudaError_t launch_scale(rg_ctx* c, double* scale_host);
+cudaError_t launch_factor(rg_ctx* c);
+cudaError_t launch_split(rg_ctx* c);
+cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r);
+cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x);
+rg_status   run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, double* acc);
+cudaError_t launch_update(rg_ctx* c, const rg_update_opts* o, double* stats);
