@@ -171,6 +171,15 @@ rg_status rg_friction(rg_ctx* ctx, double* cf_out);
  * [5] ILU apply (one), [6] update, [7] friction. */
 rg_status rg_get_timings(rg_ctx* ctx, double* ms, int n);
 
+/* Structure of the resident system: [0] neq, [1] nnz, [2] dependency depth of
+ * the L solve, [3] of the U solve, [4] element colours, [5] L entries. */
+rg_status rg_get_stats(rg_ctx* ctx, int64_t* out, int n);
+
+/* CUDA events on the context's stream (8 slots), for timing a caller's
+ * sequence of calls on the device clock. */
+rg_status rg_event_record(rg_ctx* ctx, int slot);
+rg_status rg_event_elapsed(rg_ctx* ctx, int a, int b, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

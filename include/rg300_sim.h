@@ -1,0 +1,147 @@
+/*
+ * rg300 standalone time stepping -- C ABI.
+ *
+ * Replaces EQS_UVS2D::Execute (EqsUVS2D.cpp:71-1096) for decks that the
+ * reference reads from its region/control/time-step/material files, when the
+ * caller has no reference MODEL to hand over: the library builds the wet
+ * model, boundary elements, boundary conditions, equation numbering and CRS
+ * pattern itself (MODEL::Initialize Model.cpp:121, BCONSET::InitBcon
+ * BconSet.cpp:92, EQS::SetEqno SetEqno.cpp:52, EQS::SetIndexMat
+ * IndexMat.cpp:91) and runs every Newton iteration on the GPU.
+ *
+ * Supported subset: six-node triangles, Manning friction (TYPE::friction
+ * kMANN), constant eddy viscosity (kVtConstant), no dispersion, QINLET /
+ * QTINLET discharge inlets, OUTLET water level, automatic slip walls,
+ * dry/rewet method 2 (GRID::DryRewet DryRewet.cpp:696), relaxation method 0
+ * or 2.
+ */
+#ifndef RG300_SIM_H
+#define RG300_SIM_H
+
+#include "rg300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rg_sim rg_sim;
+
+typedef enum { RG_BC_QINLET = 1, RG_BC_QTINLET = 2, RG_BC_OUTLET = 3 } rg_bc_kind;
+
+/* one $TM_LINE boundary condition (Timeint.cpp:2240-2345) */
+typedef struct {
+  int           kind;          /* rg_bc_kind */
+  int           line;          /* control-line number (material id of the line elements) */
+  int           npts;          /* 1 for QINLET/OUTLET, hydrograph length for QTINLET */
+  const double* t;             /* QTINLET times [s] */
+  const double* Q;             /* discharge [m^3/s] (inlets) */
+  const double* S;             /* water level [m] (QINLET profile level, OUTLET level) */
+} rg_line_bc;
+
+/* $RELAX, $DRYREW, $CONVERGENCE, $SOLVER, $TM_WEIGHT, physical constants */
+typedef struct {
+  double g, vk;                /* PROJECT::g, PROJECT::vk */
+  double dry_limit, rewet_limit;
+  int    dryrew_method, dryrew_freq, countdown;
+  int    relax_method;         /* 0 or 2 */
+  double max_delta_uv, max_delta_s, max_us;
+  double conv_uv, conv_s;      /* correction criterion (EqsUVS2D.cpp:436-438) */
+  int    max_newton;           /* PROJECT::actualCycit */
+  int    solver_maxiter;       /* $SOLVER maxIter */
+  double solver_maxdiff;       /* $SOLVER maxDiff */
+  double theta;                /* TIMEINT::thetaFlow */
+} rg_deck_params;
+
+typedef struct {
+  int           np;            /* region nodes */
+  const double* x;
+  const double* y;
+  const double* z;             /* bed elevation (NODE::zor) */
+  int           ne;            /* region six-node triangles */
+  const int*    elem_nodes;    /* 6 per triangle: corners ccw, then mid-sides 0-1, 1-2, 2-0 */
+  const int*    elem_mat;      /* material index per triangle */
+  int           nmat;
+  const double* mat_n;         /* Manning n ($BOTTOM no MANN n) */
+  const double* mat_vt;        /* eddy viscosity ($TURBULENCE no vt) */
+  int           nseg;          /* control-line segments (corner, corner, mid-side) */
+  const int*    seg_nodes;
+  const int*    seg_line;
+  int           nbc;
+  const rg_line_bc* bc;
+  rg_deck_params params;
+} rg_deck;
+
+typedef enum {
+  RG_CRIT_CORRECTION = 0,      /* the reference's test: max |correction| <= convUV / convS */
+  RG_CRIT_RESIDUAL   = 1       /* ||B_k||_2 / ||B_0||_2 <= residual_tol */
+} rg_criterion;
+
+typedef struct {
+  int    steady;               /* $TM_STATIONARY */
+  int    first_step;           /* first time step of the run (EQS_UVS2D::Predict) */
+  int    criterion;            /* rg_criterion */
+  double residual_tol;
+  int    max_newton;           /* 0: params.max_newton */
+} rg_step_ctl;
+
+typedef struct {
+  int    newton_iterations;
+  int    krylov_iterations;
+  int    converged;
+  int    neq;
+  int    dryrew_events;
+  int    dry_nodes;
+  int    solver_status;
+  int    n_hist;
+  double residual_first;       /* ||B_0|| */
+  double residual_ratio;       /* last ||B_k|| / ||B_0|| */
+  double wall_ms;
+  double residual_hist[64];
+} rg_step_report;
+
+/* device >= 0: GPU ordinal; RG_DEVICE_NONE: host model only (numbering and
+ * boundary set-up can be inspected, rg_sim_step is refused) */
+#define RG_DEVICE_NONE (-2)
+rg_status rg_sim_create(const rg_deck* deck, int precision, int device, rg_sim** out);
+rg_status rg_sim_destroy(rg_sim* sim);
+const char* rg_sim_last_error(rg_sim* sim);
+/* initial state ($ASC_INITFILE U V S); sets up the model as PROJECT::Compute
+ * does before its time loop (Compute.cpp:170-180) */
+rg_status rg_sim_set_state(rg_sim* sim, const double* U, const double* V, const double* S);
+rg_status rg_sim_get_state(rg_sim* sim, double* U, double* V, double* S, double* z, int* nflag);
+/* one time step [t, t+dt] (EQS_UVS2D::Execute + Compute.cpp:774-810) */
+rg_status rg_sim_step(rg_sim* sim, double t, double dt, const rg_step_ctl* ctl, rg_step_report* rep);
+/* the host part of one Newton iteration's set-up with the given nodal
+ * friction (InitBcon at time t_bc, SetLocation, SetNormal, SetRotation,
+ * SetEqno when the model changed) -- no GPU work */
+rg_status rg_sim_prepare_iteration(rg_sim* sim, double t_bc, const double* cf);
+/* one dry/rewet pass on the host state (MODEL::DoDryRewet, DoDryRew.cpp:50) --
+ * the first Newton iteration of a step starts with it */
+rg_status rg_sim_dry_rewet(rg_sim* sim, int* dried, int* wetted);
+/* the numbering, pattern and boundary data of the last Newton iteration */
+rg_status rg_sim_get_numbering(rg_sim* sim, int* neq, int* eqno, int* width, int64_t* nnz);
+rg_status rg_sim_get_pattern(rg_sim* sim, int* index);
+rg_status rg_sim_get_boundary(rg_sim* sim, int* nflag, int* bckind, double* rot4, double* bcU, double* bcS);
+
+/* the GPU context of a simulation (for rg_get_stats, rg_event_*, timings) */
+rg_ctx* rg_sim_context(rg_sim* sim);
+
+/* context-level helpers used by the time stepper (also usable by a caller that
+ * drives rg_ctx itself) */
+/* replace the model element list (MODEL::Initialize after dry/rewet) */
+rg_status rg_set_elements(rg_ctx* ctx, int ne, const int* elem_nodes, const int* elem_nnd,
+                          const int* elem_flag, const double* elem_vt);
+/* previous time level NODE::vo (U, V, S and their time derivatives) */
+rg_status rg_set_old(rg_ctx* ctx, const double* U, const double* V, const double* S,
+                     const double* dUdt, const double* dVdt, const double* dSdt);
+rg_status rg_get_dt(rg_ctx* ctx, double* dUdt, double* dVdt, double* dSdt);
+/* EQS_UVS2D::Timegrad (EqsUVS2D.cpp:1183-1230) on the device state */
+rg_status rg_timegrad(rg_ctx* ctx, double dt, double theta);
+/* U = V = 0 at the listed nodes (kNoMoment, Transform.cpp:441-449) */
+rg_status rg_zero_velocity(rg_ctx* ctx, int n, const int* nodes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -87,7 +87,7 @@ class Model:
 def model_from_state(st: dict) -> Model:
     """orc_model inputs from a STATE record of the reference dump."""
     mats = st["materials"]
-    evt = mats[:, 3][np.clip(st["elem_type"], 0, len(mats) - 1)]
+    evt = mats[:, 3][np.clip(st["elem_type"] - 1, 0, len(mats) - 1)]   # 1-based TYPE ids
     rot = np.stack([st["r00"], st["r01"], st["r10"], st["r11"]], axis=1)
     eqno = np.stack([st["eq0"], st["eq1"], st["eq2"]], axis=1)
     return Model(x=st["x"], y=st["y"], z=st["z"], U=st["U"], V=st["V"], S=st["S"],

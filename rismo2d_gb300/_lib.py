@@ -30,7 +30,12 @@ PREC_MIXED = 2
 EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pattern", "rg_set_boundary",
            "rg_set_state", "rg_get_state", "rg_set_relax", "rg_assemble", "rg_load_system", "rg_scale",
            "rg_ilu0_factor", "rg_ilu0_apply", "rg_spmv", "rg_bicgstab", "rg_solve", "rg_set_update_lists",
-           "rg_newton_update", "rg_set_friction", "rg_friction", "rg_get_timings"]
+           "rg_newton_update", "rg_set_friction", "rg_friction", "rg_get_timings",
+           "rg_sim_create", "rg_sim_destroy", "rg_sim_last_error", "rg_sim_set_state", "rg_sim_get_state",
+           "rg_sim_step", "rg_sim_prepare_iteration", "rg_sim_get_numbering", "rg_sim_get_pattern",
+           "rg_sim_get_boundary", "rg_set_elements", "rg_set_old", "rg_get_dt", "rg_timegrad",
+           "rg_zero_velocity", "rg_sim_dry_rewet", "rg_get_stats", "rg_event_record", "rg_event_elapsed",
+           "rg_sim_context"]
 
 
 class RgMesh(C.Structure):

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librg300.so")
-SOURCES = ["rg_assemble.cu", "rg_linalg.cu", "rg_api.cu"]
+SOURCES = ["rg_assemble.cu", "rg_linalg.cu", "rg_api.cu", "rg_model.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -31,10 +31,14 @@ def _nvcc() -> str:
 def _compile(src: str) -> str:
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     deps = [os.path.join(CSRC, src), os.path.join(CSRC, "rg_internal.cuh"),
-            os.path.join(HERE, "..", "include", "rg300.h")]
+            os.path.join(HERE, "..", "include", "rg300.h"), os.path.join(HERE, "..", "include", "rg300_sim.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
-    subprocess.check_call([_nvcc()] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
+    if src.endswith(".cpp"):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I/usr/local/cuda/include", "-c"]
+    else:
+        cmd = [_nvcc()] + ARCH + FLAGS + ["-c"]
+    subprocess.check_call(cmd + [os.path.join(CSRC, src), "-o", obj])
     return obj
 
 

@@ -172,6 +172,31 @@ __global__ void k_upd_midside(int ner, const int* __restrict__ rnodes, double* S
   }
 }
 
+// EQS_UVS2D::Timegrad (EqsUVS2D.cpp:1183-1230)
+__global__ void k_timegrad(int np, const int* __restrict__ nflag, const double* U, const double* V, const double* S,
+                           const double* oU, const double* oV, const double* oS, const double* odU,
+                           const double* odV, const double* odS, double* dU, double* dV, double* dS, double iTheta,
+                           double thdt) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += gridDim.x * blockDim.x) {
+    // kDry | kDryPrev | kMarsh | kMarshPrev
+    if (nflag[n] & (64 | 128 | 256 | 512)) {
+      dU[n] = dV[n] = dS[n] = 0.0;
+    } else {
+      dU[n] = iTheta * odU[n] + thdt * (U[n] - oU[n]);
+      dV[n] = iTheta * odV[n] + thdt * (V[n] - oV[n]);
+      dS[n] = iTheta * odS[n] + thdt * (S[n] - oS[n]);
+    }
+  }
+}
+
+__global__ void k_zero_uv(int n, const int* nodes, double* U, double* V) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    U[nodes[i]] = 0.0;
+    V[nodes[i]] = 0.0;
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_update(rg_ctx* c, const rg_update_opts* o, double* stats) {
@@ -407,6 +432,27 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
   TRY(upload(c, c->Uptr, Uptr.data(), Uptr.size()));
   TRY(upload(c, c->Ucol, Ucol.data(), Ucol.size()));
   TRY(upload(c, c->Usrc, Usrc.data(), Usrc.size()));
+  // longest dependency chains of the L and U solves (level-set depths)
+  {
+    std::vector<int> lev(neq, 0);
+    int dl = 0;
+    for (int i = 0; i < neq; i++) {
+      int l = 0;
+      for (int q = Lptr[i]; q < Lptr[i + 1]; q++) l = std::max(l, lev[Lcol[q]] + 1);
+      lev[i] = l;
+      dl = std::max(dl, l + 1);
+    }
+    int du = 0;
+    for (int i = neq - 1; i >= 0; i--) {
+      int l = 0;
+      for (int q = Uptr[i]; q < Uptr[i + 1]; q++) l = std::max(l, lev[Ucol[q]] + 1);
+      lev[i] = l;
+      du = std::max(du, l + 1);
+    }
+    c->depth_L = dl;
+    c->depth_U = du;
+    c->n_colors = ncol;
+  }
   TRY(c->fflag.alloc(neq));
   TRY(cudaMemsetAsync(c->fflag.p, 0, neq * sizeof(int), c->st));
   c->fepoch = 0;
@@ -726,6 +772,109 @@ rg_status rg_friction(rg_ctx* c, double* cf_out) {
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[14], c->ev[15]));
   c->t_ms[7] = ms;
+  return RG_OK;
+}
+
+rg_status rg_set_elements(rg_ctx* c, int ne, const int* elem_nodes, const int* elem_nnd, const int* elem_flag,
+                          const double* elem_vt) {
+  if (!c || ne <= 0 || !elem_nodes || !elem_nnd || !elem_flag || !elem_vt)
+    return rg_fail(c, RG_ERR_ARG, "rg_set_elements: bad arguments");
+  for (int e = 0; e < ne; e++) {
+    if (elem_nnd[e] != 6 && elem_nnd[e] != 3) return rg_fail(c, RG_ERR_ARG, "rg_set_elements: bad node count");
+    for (int i = 0; i < elem_nnd[e]; i++)
+      if (elem_nodes[6 * e + i] < 0 || elem_nodes[6 * e + i] >= c->np)
+        return rg_fail(c, RG_ERR_ARG, "rg_set_elements: node out of range");
+  }
+  TRY(cudaSetDevice(c->device));
+  c->ne = ne;
+  TRY(upload(c, c->enodes, elem_nodes, 6 * (size_t)ne));
+  TRY(upload(c, c->ennd, elem_nnd, ne));
+  TRY(upload(c, c->eflag, elem_flag, ne));
+  TRY(upload(c, c->evt, elem_vt, ne));
+  c->h_enodes.assign(elem_nodes, elem_nodes + 6 * (size_t)ne);
+  c->h_ennd.assign(elem_nnd, elem_nnd + ne);
+  c->h_eflag.assign(elem_flag, elem_flag + ne);
+  c->neq = 0;   // a pattern for the new element list must follow
+  c->have_system = c->have_factor = false;
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_set_old(rg_ctx* c, const double* U, const double* V, const double* S, const double* dUdt,
+                     const double* dVdt, const double* dSdt) {
+  if (!c) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  const size_t np = c->np;
+  TRY(upload_if(c, c->oU, U, np));
+  TRY(upload_if(c, c->oV, V, np));
+  TRY(upload_if(c, c->oS, S, np));
+  TRY(upload_if(c, c->odUdt, dUdt, np));
+  TRY(upload_if(c, c->odVdt, dVdt, np));
+  TRY(upload_if(c, c->odSdt, dSdt, np));
+  return RG_OK;
+}
+
+rg_status rg_get_dt(rg_ctx* c, double* dUdt, double* dVdt, double* dSdt) {
+  if (!c) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  const size_t b = c->np * sizeof(double);
+  if (dUdt) TRY(cudaMemcpyAsync(dUdt, c->dUdt.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (dVdt) TRY(cudaMemcpyAsync(dVdt, c->dVdt.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (dSdt) TRY(cudaMemcpyAsync(dSdt, c->dSdt.p, b, cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+rg_status rg_timegrad(rg_ctx* c, double dt, double theta) {
+  if (!c || !c->oU.p || !(dt > 0.0) || !(fabs(theta) > 1.0e-10))
+    return rg_fail(c, RG_ERR_ARG, "rg_timegrad: previous time level not set");
+  TRY(cudaSetDevice(c->device));
+  const double iTheta = 1.0 - 1.0 / theta, thdt = 1.0 / dt / theta;
+  int nb = (c->np + 255) / 256;
+  if (nb > c->num_sms * 8) nb = c->num_sms * 8;
+  k_timegrad<<<nb, 256, 0, c->st>>>(c->np, c->nflag.p, c->U.p, c->V.p, c->S.p, c->oU.p, c->oV.p, c->oS.p,
+                                    c->odUdt.p, c->odVdt.p, c->odSdt.p, c->dUdt.p, c->dVdt.p, c->dSdt.p, iTheta,
+                                    thdt);
+  TRY(cudaGetLastError());
+  return RG_OK;
+}
+
+rg_status rg_zero_velocity(rg_ctx* c, int n, const int* nodes) {
+  if (!c || n < 0 || (n && !nodes)) return RG_ERR_ARG;
+  if (n == 0) return RG_OK;
+  for (int i = 0; i < n; i++)
+    if (nodes[i] < 0 || nodes[i] >= c->np) return rg_fail(c, RG_ERR_ARG, "rg_zero_velocity: node out of range");
+  TRY(cudaSetDevice(c->device));
+  TRY(upload(c, c->zero_nodes, nodes, n));
+  k_zero_uv<<<(n + 255) / 256, 256, 0, c->st>>>(n, c->zero_nodes.p, c->U.p, c->V.p);
+  TRY(cudaGetLastError());
+  return RG_OK;
+}
+
+rg_status rg_get_stats(rg_ctx* c, int64_t* out, int n) {
+  if (!c || !out) return RG_ERR_ARG;
+  int64_t v[6] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n};
+  for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+  return RG_OK;
+}
+
+rg_status rg_event_record(rg_ctx* c, int slot) {
+  if (!c || slot < 0 || slot >= 8) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  if (!c->user_ev_ready) {
+    for (int i = 0; i < 8; i++) TRY(cudaEventCreate(&c->user_ev[i]));
+    c->user_ev_ready = true;
+  }
+  TRY(cudaEventRecord(c->user_ev[slot], c->st));
+  return RG_OK;
+}
+
+rg_status rg_event_elapsed(rg_ctx* c, int a, int b, double* ms) {
+  if (!c || !c->user_ev_ready || a < 0 || b < 0 || a >= 8 || b >= 8 || !ms) return RG_ERR_ARG;
+  TRY(cudaEventSynchronize(c->user_ev[b]));
+  float f = 0;
+  TRY(cudaEventElapsedTime(&f, c->user_ev[a], c->user_ev[b]));
+  *ms = f;
   return RG_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "../../include/rg300.h"
+#include "../../include/rg300_sim.h"
 
 #include <cuda_runtime.h>
 
@@ -76,6 +77,8 @@ struct rg_ctx {
 
   // node state and boundary data
   DBuf<double> U, V, S, dUdt, dVdt, dSdt, z, cf, cfw;
+  DBuf<double> oU, oV, oS, odUdt, odVdt, odSdt;   // previous time level (NODE::vo)
+  DBuf<int> zero_nodes;
   DBuf<int> nflag, bckind;
   DBuf<double> rot, niox, nioy, bcU, bcS;
   bool have_boundary = false;
@@ -127,6 +130,9 @@ struct rg_ctx {
   double t_ms[8] = {0};
 
   int persist_blocks = 0;    // co-resident blocks for the persistent kernels
+  int depth_L = 0, depth_U = 0, n_colors = 0;   // dependency depth of the triangular solves
+  cudaEvent_t user_ev[8];
+  bool user_ev_ready = false;
 };
 
 // ---- launchers implemented in the .cu files -------------------------------

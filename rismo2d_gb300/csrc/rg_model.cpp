@@ -1,0 +1,1148 @@
+// Host-side model of a shallow-water time step: the per-iteration bookkeeping
+// of EQS_UVS2D::Execute (EqsUVS2D.cpp:71-1096) around the GPU hot path.
+//
+// Restated reference routines (host, changes only with the wet/dry state or
+// the boundary data):
+//   GRID::Connection        Connect.cpp:43-126     node -> wet element counts
+//   MODEL::Boundary         Bound.cpp:50-164       boundary line elements
+//   MODEL::Initialize       Model.cpp:121-216      wet node / element lists
+//   MODEL::SetLocation      Locate.cpp:47-193      inlet/outlet/convex flags
+//   MODEL::SetNormal        Transform.cpp:52-265   boundary normals
+//   MODEL::SetRotation      Transform.cpp:269-498  slip / normal-flow rotation
+//   BCONSET::InitBcon       BconSet.cpp:92-487     node boundary conditions
+//   BCONLINE::Inlet/Outlet  BconLine.cpp:249-985   QINLET, QTINLET, OUTLET
+//   EQS::SetEqno            SetEqno.cpp:52-543     numbering + frontal order
+//   EQS::SetIndexMat        IndexMat.cpp:91-342    CRS pattern
+//   GRID::DryRewet          DryRewet.cpp:696-990   dry/rewet method 2
+//   GRID::AreaFactors       ArFact.cpp:41-97       inclined-element factor
+//   EQS_UVS2D::Predict      EqsUVS2D.cpp:1101-1178
+//   GRID::SetSlipFlow       SlipFlow.cpp:42-80
+// The hot path (friction, assembly, scaling, ILU(0), BiCGStab, correction,
+// time derivatives) runs on the GPU through the rg_* entry points.
+
+#include "rg_internal.cuh"
+#include "../../include/rg300_sim.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace {
+
+// NODE::flag (Node.h)
+enum : unsigned {
+  N_INLET = 1, N_OUTLET = 2, N_OPENBND = 4, N_GRIDBND = 8, N_BOUND = 16, N_ROTAT = 32, N_DRY = 64,
+  N_DRYPREV = 128, N_MARSH = 256, N_MARSHPREV = 512, N_CORN = 1024, N_MIDS = 2048, N_NOMOMENT = 4096
+};
+// ELEM::flag (Elem.h)
+enum : unsigned {
+  E_INLET = 1, E_OUTLET = 2, E_OPENBND = 4, E_BOUND = 16, E_REGION = 32, E_DRY = 128, E_DRYPREV = 256,
+  E_MARSH = 512, E_MARSHPREV = 1024
+};
+// BCON::kind (Bcon.h)
+enum : unsigned {
+  B_INLET = 1, B_OUTLET = 2, B_OPENBND = 4, B_QINLET = 8, B_QTINLET = 16, B_SLIP = 128, B_SETUV = 512,
+  B_SETS = 1024, B_FIXU = 32768, B_FIXV = 65536, B_AUTOSLIP = 4194304
+};
+enum { ROT_NONE = 0, ROT_TANGENT = 1, ROT_NORMAL = 2 };
+
+struct BElem {       // boundary line element (corner, corner, mid-side)
+  int nd[3];
+  unsigned flag;
+  int region;        // owning region triangle
+};
+
+struct LineBc {
+  int line = 0;
+  unsigned kind = 0;
+  std::vector<double> t, Q, S;   // QINLET: one row; QTINLET: hydrograph
+};
+
+double interp_hydro(const LineBc& b, double t, double* Sspec) {
+  // BCONLINE::FindInterval on time (BconLine.cpp:167-227), linear in between
+  double Q = b.Q[0];
+  *Sspec = b.S[0];
+  const int n = (int)b.t.size();
+  for (int i = 0; i < n - 1; i++) {
+    double dx = b.t[i + 1] - b.t[i];
+    double lx = t - b.t[i];
+    if (std::fabs(dx) > 1.0e-20)
+      lx /= dx;
+    else
+      lx = dx = 0.0;
+    bool hit;
+    double L;
+    if (std::fabs(dx) < 1.0e-20 && std::fabs(lx) < 1.0e-20) {
+      hit = true;   // ly == 0 for a time series
+      L = 0.0;
+    } else {
+      hit = (lx > -0.001 && lx < 1.001);
+      L = lx;
+    }
+    if (hit) {
+      Q = b.Q[i] + L * (b.Q[i + 1] - b.Q[i]);
+      *Sspec = b.S[i] + L * (b.S[i + 1] - b.S[i]);
+      return Q;
+    }
+  }
+  return Q;
+}
+
+}  // namespace
+
+struct rg_sim {
+  rg_ctx* ctx = nullptr;
+  int prec = RG_PREC_FP64;
+  std::string err;
+
+  // region
+  int np = 0, ne = 0;
+  std::vector<double> x, y, zor, z;
+  std::vector<int> en;           // 6 per region triangle
+  std::vector<double> en_n, en_vt, en_af;
+  std::vector<unsigned> eflag, nflag;
+  std::vector<int> noel, countdown;
+  // control lines
+  std::vector<int> seg_nodes, seg_line;
+  std::vector<LineBc> bcl;
+  // per-node boundary data
+  std::vector<unsigned> bckind;
+  std::vector<int> rot, has_val;
+  std::vector<double> bnx, bny, niox, nioy, bcU, bcS;
+  // state (host mirror)
+  std::vector<double> U, V, S, dUdt, dVdt, dSdt, oU, oV, oS, odUdt, odVdt, odSdt, cf;
+  // boundary elements, model lists
+  std::vector<BElem> bel;
+  std::vector<int> boundList;    // mid-side node -> boundary element
+  std::vector<int> mnodes;       // wet nodes
+  std::vector<int> melems;       // >= 0 region triangle, < 0: -(1+boundary element)
+  int model_init = 0, eqs_init = -1;
+  bool firstDryRew = true;
+  // numbering and pattern
+  int neq = 0;
+  std::vector<int> eqno;         // 3 per node
+  std::vector<int> width, index;
+  // parameters
+  rg_deck_params p{};
+  double hmin = 0.0;
+  bool have_state = false;
+  // last step report detail
+  std::vector<double> resid_hist;
+};
+
+static rg_status sfail(rg_sim* s, rg_status st, const std::string& m) {
+  s->err = m;
+  return st;
+}
+
+// ---- MODEL::Initialize and helpers ----------------------------------------
+
+static void connection(rg_sim* s, unsigned dry) {
+  std::fill(s->noel.begin(), s->noel.end(), 0);
+  for (int e = 0; e < s->ne; e++) {
+    if (dry && (s->eflag[e] & dry)) continue;
+    for (int i = 0; i < 6; i++) s->noel[s->en[6 * e + i]]++;
+  }
+}
+
+static void boundary(rg_sim* s) {
+  for (int n = 0; n < s->np; n++) {
+    s->nflag[n] &= ~N_BOUND;
+    if (s->bckind[n] & B_AUTOSLIP) s->bckind[n] &= ~(B_AUTOSLIP | B_FIXU | B_FIXV);
+  }
+  for (int n = 0; n < s->np; n++)
+    if (s->noel[n] == 1 && (s->nflag[n] & N_MIDS)) s->nflag[n] |= N_BOUND;
+  s->bel.clear();
+  std::fill(s->boundList.begin(), s->boundList.end(), -1);
+  for (int e = 0; e < s->ne; e++) {
+    if (s->eflag[e] & E_DRY) continue;
+    const int* nd = &s->en[6 * e];
+    for (int i = 3; i < 6; i++) {
+      if (!(s->nflag[nd[i]] & N_BOUND)) continue;
+      int left = i - 3, rght = (left + 1) % 3;
+      BElem b;
+      b.nd[0] = nd[left];
+      b.nd[1] = nd[rght];
+      b.nd[2] = nd[i];
+      b.flag = E_BOUND;
+      b.region = e;
+      s->boundList[nd[i]] = (int)s->bel.size();
+      s->nflag[nd[left]] |= N_BOUND;
+      s->nflag[nd[rght]] |= N_BOUND;
+      s->bel.push_back(b);
+    }
+  }
+}
+
+static void set_location(rg_sim* s) {
+  for (BElem& b : s->bel) {
+    bool inlet = true, outlet = true, open = true;
+    for (int i = 0; i < 2; i++) {
+      unsigned k = s->bckind[b.nd[i]];
+      if (!(k & B_INLET)) inlet = false;
+      if (!(k & B_OUTLET)) outlet = false;
+      if (!(k & B_OPENBND)) open = false;
+    }
+    if (inlet) b.flag |= E_INLET;
+    if (outlet) b.flag |= E_OUTLET;
+    if (open) b.flag |= E_OPENBND;
+    for (int i = 0; i < 3; i++) {
+      if (inlet) s->nflag[b.nd[i]] |= N_INLET;
+      if (outlet) s->nflag[b.nd[i]] |= N_OUTLET;
+      if (open) s->nflag[b.nd[i]] |= N_OPENBND;
+    }
+  }
+  for (int n = 0; n < s->np; n++) s->nflag[n] &= ~N_NOMOMENT;
+  for (BElem& b : s->bel)
+    for (int i = 0; i < 2; i++) {
+      int k = b.nd[i];
+      if (s->noel[k] == 1 && !(s->nflag[k] & (N_INLET | N_OUTLET | N_OPENBND))) s->nflag[k] |= N_NOMOMENT;
+    }
+}
+
+static void initialize(rg_sim* s) {
+  s->model_init++;
+  connection(s, E_DRY);
+  boundary(s);
+  s->mnodes.clear();
+  for (int n = 0; n < s->np; n++)
+    if (!(s->nflag[n] & N_DRY)) s->mnodes.push_back(n);
+  s->melems.clear();
+  for (int e = 0; e < s->ne; e++) {
+    if (s->eflag[e] & E_DRY) continue;
+    s->melems.push_back(e);
+    for (int i = 3; i < 6; i++) {
+      int k = s->en[6 * e + i];
+      if (s->nflag[k] & N_BOUND) s->melems.push_back(-1 - s->boundList[k]);
+    }
+  }
+  set_location(s);
+}
+
+// ---- MODEL::SetNormal / SetRotation ----------------------------------------
+
+static void set_normal(rg_sim* s) {
+  std::fill(s->bnx.begin(), s->bnx.end(), 0.0);
+  std::fill(s->bny.begin(), s->bny.end(), 0.0);
+  std::fill(s->niox.begin(), s->niox.end(), 0.0);
+  std::fill(s->nioy.begin(), s->nioy.end(), 0.0);
+  // derivatives of the quadratic line shape at its nodes (xi = -1, 1, 0)
+  const double xi[3] = {-1.0, 1.0, 0.0};
+  for (const BElem& b : s->bel) {
+    for (int i = 0; i < 3; i++) {
+      double d[3] = {xi[i] - 0.5, xi[i] + 0.5, -2.0 * xi[i]};
+      double nx = 0.0, ny = 0.0;
+      for (int j = 0; j < 3; j++) {
+        nx += 2.0 * (d[j] * s->y[b.nd[j]]);
+        ny -= 2.0 * (d[j] * s->x[b.nd[j]]);
+      }
+      int k = b.nd[i];
+      if (b.flag & (E_INLET | E_OUTLET | E_OPENBND)) {
+        s->niox[k] += nx;
+        s->nioy[k] += ny;
+      } else {
+        s->bnx[k] += nx;
+        s->bny[k] += ny;
+      }
+    }
+  }
+  for (int n = 0; n < s->np; n++) {
+    if (s->nflag[n] & N_DRY) continue;
+    if (!(s->nflag[n] & N_BOUND)) continue;
+    double len = std::sqrt(s->bnx[n] * s->bnx[n] + s->bny[n] * s->bny[n]);
+    if (std::fabs(len) < 1.0e-12) {
+      s->bnx[n] = s->bny[n] = 0.0;
+    } else {
+      s->bnx[n] /= len;
+      s->bny[n] /= len;
+    }
+    len = std::sqrt(s->niox[n] * s->niox[n] + s->nioy[n] * s->nioy[n]);
+    if (std::fabs(len) < 1.0e-12) {
+      s->niox[n] = s->nioy[n] = 0.0;
+    } else {
+      s->niox[n] /= len;
+      s->nioy[n] /= len;
+    }
+  }
+}
+
+static void set_rotation(rg_sim* s, std::vector<int>* zero_uv) {
+  for (int n = 0; n < s->np; n++) {
+    s->nflag[n] &= ~N_ROTAT;
+    s->rot[n] = ROT_NONE;
+    unsigned& k = s->bckind[n];
+    if (k & B_INLET) k &= ~(B_FIXU | B_FIXV);
+    if (k & B_AUTOSLIP) k &= ~(B_AUTOSLIP | B_FIXU | B_FIXV);
+    bool bound = (s->nflag[n] & N_BOUND) != 0;
+    if (bound && !(k & (B_INLET | B_OUTLET | B_OPENBND | B_SLIP | B_SETUV))) {
+      s->rot[n] = ROT_TANGENT;
+      k |= B_AUTOSLIP | B_FIXV;
+    }
+  }
+  for (const BElem& b : s->bel) {
+    if (b.flag & (E_OUTLET | E_OPENBND)) continue;
+    for (int i = 0; i < 2; i++) {
+      int n = b.nd[i];
+      unsigned& k = s->bckind[n];
+      if ((k & (B_OUTLET | B_OPENBND)) && !(k & (B_SLIP | B_SETUV))) {
+        s->rot[n] = ROT_NORMAL;
+        k |= B_AUTOSLIP | B_FIXV;
+      }
+    }
+  }
+  for (int n = 0; n < s->np; n++) {
+    if (s->bckind[n] & B_AUTOSLIP) {
+      double len = std::sqrt(s->bnx[n] * s->bnx[n] + s->bny[n] * s->bny[n]);
+      if (len < 1.0e-12) s->nflag[n] |= N_NOMOMENT;
+    }
+  }
+  for (int n = 0; n < s->np; n++) {
+    unsigned& k = s->bckind[n];
+    if (k & B_INLET) {
+      s->nflag[n] |= N_ROTAT;
+      k |= B_FIXV;
+      s->rot[n] = ROT_NORMAL;
+    }
+    if ((s->nflag[n] & N_NOMOMENT) && !(k & (B_SETUV | B_OUTLET | B_OPENBND))) {
+      k |= B_AUTOSLIP | B_FIXU | B_FIXV;
+      s->U[n] = s->V[n] = 0.0;
+      if (zero_uv) zero_uv->push_back(n);
+    } else if ((k & B_FIXV) && (k & B_AUTOSLIP)) {
+      s->nflag[n] |= N_ROTAT;
+      s->rot[n] = (k & (B_OUTLET | B_OPENBND)) ? ROT_NORMAL : ROT_TANGENT;
+    }
+  }
+}
+
+static void getrot(const rg_sim* s, int n, double r[4]) {
+  // BCON::Getrot (Bcon.cpp:209-238)
+  switch (s->rot[n]) {
+    case ROT_TANGENT:
+      r[0] = s->bny[n];
+      r[1] = s->bnx[n];
+      r[2] = -s->bnx[n];
+      r[3] = s->bny[n];
+      break;
+    case ROT_NORMAL:
+      r[0] = s->niox[n];
+      r[1] = s->nioy[n];
+      r[2] = s->nioy[n];
+      r[3] = -s->niox[n];
+      break;
+    default:
+      r[0] = r[1] = r[2] = r[3] = 0.0;
+  }
+}
+
+// ---- BCONSET::InitBcon ------------------------------------------------------
+
+// returns true when the inlet was dry and its water level was initialised
+static bool init_bcon(rg_sim* s, double t) {
+  bool s_changed = false;
+  const int np = s->np;
+  std::vector<unsigned> kind(np, 0);
+  std::vector<char> has(np, 0);
+  std::vector<double> vU(np, 0.0), vS(np, 0.0);
+  std::vector<char> mark(np, 0);
+  for (const LineBc& b : s->bcl) {
+    std::fill(mark.begin(), mark.end(), 0);
+    unsigned k = b.kind;
+    if (k & B_QTINLET) k |= B_QINLET;
+    if (k & B_QINLET) k |= B_INLET;
+    if (k & B_INLET) {
+      // BCONLINE::Inlet, QINLET / QTINLET (BconLine.cpp:260-511)
+      double Sspec = b.S[0];
+      double Qspec = (k & B_QTINLET) ? interp_hydro(b, t, &Sspec) : b.Q[0];
+      double Q = 0.0;
+      bool any = false;
+      const double gx = std::sqrt(0.6);
+      const double gp[3] = {-gx, 0.0, gx}, gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+      for (size_t c = 0; c < s->seg_line.size(); c++) {
+        if (s->seg_line[c] != b.line) continue;
+        const int* nd = &s->seg_nodes[3 * c];
+        double q[3];
+        for (int i = 0; i < 3; i++) {
+          int n = nd[i];
+          if (s->S[n] - s->z[n] < 1.0e-9 || (s->nflag[n] & (N_DRY | N_MARSH))) {
+            q[i] = 0.0;
+          } else {
+            double h = Sspec - s->z[n];
+            q[i] = (h > 0.0) ? std::sqrt(h * h * h) : 0.0;
+            if (s->cf[n] > 0.0) q[i] /= std::sqrt(s->cf[n]);
+            any = true;
+          }
+          mark[n] = 1;
+        }
+        for (int g = 0; g < 3; g++) {
+          double x = gp[g];
+          double N[3] = {x * (x - 1.0) / 2.0, x * (x + 1.0) / 2.0, 1.0 - x * x};
+          double dN[3] = {x - 0.5, x + 0.5, -2.0 * x};
+          double dx = dN[0] * s->x[nd[0]] + dN[1] * s->x[nd[1]] + dN[2] * s->x[nd[2]];
+          double dy = dN[0] * s->y[nd[0]] + dN[1] * s->y[nd[1]] + dN[2] * s->y[nd[2]];
+          double qg = N[0] * q[0] + N[1] * q[1] + N[2] * q[2];
+          Q += gw[g] * std::sqrt(dx * dx + dy * dy) * qg;
+        }
+      }
+      double Qratio = (std::fabs(Q) > 0.0) ? (-Qspec / Q) : 0.0;
+      if (!any) {
+        // dry inlet: initialise S along the line, integrate on zor (BconLine.cpp:380-455)
+        Q = 0.0;
+        for (size_t c = 0; c < s->seg_line.size(); c++) {
+          if (s->seg_line[c] != b.line) continue;
+          const int* nd = &s->seg_nodes[3 * c];
+          double q[3];
+          for (int i = 0; i < 3; i++) {
+            s->S[nd[i]] = Sspec;
+            double h = Sspec - s->zor[nd[i]];
+            q[i] = (h > 0.0) ? std::sqrt(h * h * h) : 0.0;
+          }
+          for (int g = 0; g < 3; g++) {
+            double x = gp[g];
+            double N[3] = {x * (x - 1.0) / 2.0, x * (x + 1.0) / 2.0, 1.0 - x * x};
+            double dN[3] = {x - 0.5, x + 0.5, -2.0 * x};
+            double dx = dN[0] * s->x[nd[0]] + dN[1] * s->x[nd[1]] + dN[2] * s->x[nd[2]];
+            double dy = dN[0] * s->y[nd[0]] + dN[1] * s->y[nd[1]] + dN[2] * s->y[nd[2]];
+            double qg = N[0] * q[0] + N[1] * q[1] + N[2] * q[2];
+            Q += gw[g] * std::sqrt(dx * dx + dy * dy) * qg;
+          }
+        }
+        Qratio = (std::fabs(Q) > 0.0) ? (-Qspec / Q) : 0.0;
+        s_changed = true;
+      }
+      for (int n = 0; n < np; n++) {
+        if (!mark[n]) continue;
+        double qn = 0.0;
+        if (!(s->nflag[n] & (N_DRY | N_MARSH))) {
+          double h = Sspec - s->z[n];
+          qn = (h > 0.0) ? std::sqrt(h * h * h) : 0.0;
+          if (s->cf[n] > 0.0) qn /= std::sqrt(s->cf[n]);
+        }
+        if (!has[n]) {
+          kind[n] = k;
+          has[n] = 1;
+          vU[n] = qn * Qratio;
+          vS[n] = Sspec;
+        } else if (!(kind[n] & (B_OUTLET | B_SLIP | B_SETUV))) {
+          kind[n] |= k;
+          vU[n] = qn * Qratio;
+          vS[n] = Sspec;
+        }
+      }
+    } else if (k & B_OUTLET) {
+      // BCONLINE::Outlet, constant S along the line (BconLine.cpp:861-903)
+      for (size_t c = 0; c < s->seg_line.size(); c++) {
+        if (s->seg_line[c] != b.line) continue;
+        const int* nd = &s->seg_nodes[3 * c];
+        for (int i = 0; i < 3; i++) {
+          int n = nd[i];
+          if (mark[n]) continue;
+          mark[n] = 1;
+          if (!has[n]) {
+            kind[n] = k;
+            has[n] = 1;
+            vS[n] = b.S[0];
+          } else if (!(kind[n] & (B_INLET | B_QINLET | B_QTINLET))) {
+            kind[n] |= k;
+            vS[n] = b.S[0];
+          }
+        }
+      }
+    }
+  }
+  for (int n = 0; n < np; n++) {
+    unsigned k = kind[n];
+    if (has[n] && (k & B_INLET)) k &= ~(B_OUTLET | B_SLIP | B_SETUV);
+    s->bckind[n] = has[n] ? k : 0;
+    s->has_val[n] = has[n];
+    s->bcU[n] = has[n] ? vU[n] : 0.0;
+    s->bcS[n] = has[n] ? vS[n] : 0.0;
+  }
+  return s_changed;
+}
+
+// ---- EQS::SetEqno / LastEquation / ResetEqOrder / SetIndexMat ----------------
+
+static void elem_nodes(const rg_sim* s, int me, const int** nd, int* nnd) {
+  if (me >= 0) {
+    *nd = &s->en[6 * me];
+    *nnd = 6;
+  } else {
+    *nd = s->bel[-1 - me].nd;
+    *nnd = 3;
+  }
+}
+
+static rg_status set_eqno(rg_sim* s) {
+  const unsigned fix[3] = {B_FIXU, B_FIXV, B_SETS};
+  std::vector<int>& eq = s->eqno;
+  std::fill(eq.begin(), eq.end(), -1);
+  int neq = 0;
+  for (int n : s->mnodes) {
+    if (s->nflag[n] & N_CORN) {
+      for (int j = 0; j < 3; j++)
+        if (!(s->bckind[n] & fix[j])) eq[3 * n + j] = neq++;
+    } else {
+      for (int j = 0; j < 2; j++)
+        if (!(s->bckind[n] & fix[j])) eq[3 * n + j] = neq++;
+    }
+  }
+  // last occurrence of every equation in element order (SetEqno.cpp:231-384)
+  std::vector<int> counter(neq, 0);
+  const size_t nme = s->melems.size();
+  for (size_t e = 0; e < nme; e++) {
+    const int* nd;
+    int nnd;
+    elem_nodes(s, s->melems[e], &nd, &nnd);
+    for (int i = 0; i < nnd; i++)
+      for (int j = 0; j < 3; j++) {
+        int q = eq[3 * nd[i] + j];
+        if (q >= 0) counter[q]++;
+      }
+  }
+  std::vector<int> ord(neq, -1);
+  int m = 0;
+  for (size_t e = 0; e < nme; e++) {
+    const int* nd;
+    int nnd;
+    elem_nodes(s, s->melems[e], &nd, &nnd);
+    for (int i = 0; i < nnd; i++)
+      for (int j = 0; j < 3; j++) {
+        int q = eq[3 * nd[i] + j];
+        if (q >= 0) {
+          if (--counter[q] == 0) ord[q] = m++;
+        }
+      }
+  }
+  if (m != neq) return sfail(s, RG_ERR_ARG, "equation numbering: inconsistent last occurrences");
+  for (size_t k = 0; k < eq.size(); k++)
+    if (eq[k] >= 0) eq[k] = ord[eq[k]];
+  s->neq = neq;
+  // CRS pattern, diagonal first then first-seen columns (IndexMat.cpp:126-288)
+  std::vector<std::vector<int>> rows(neq);
+  for (size_t e = 0; e < nme; e++) {
+    const int* nd;
+    int nnd;
+    elem_nodes(s, s->melems[e], &nd, &nnd);
+    for (int i = 0; i < nnd; i++)
+      for (int j = 0; j < 3; j++) {
+        int row = eq[3 * nd[i] + j];
+        if (row < 0) continue;
+        std::vector<int>& r = rows[row];
+        if (r.empty()) r.push_back(row);
+        for (int k = 0; k < nnd; k++)
+          for (int l = 0; l < 3; l++) {
+            int col = eq[3 * nd[k] + l];
+            if (col < 0) continue;
+            if (std::find(r.begin(), r.end(), col) == r.end()) r.push_back(col);
+          }
+      }
+  }
+  s->width.assign(neq, 0);
+  s->index.clear();
+  for (int i = 0; i < neq; i++) {
+    s->width[i] = (int)rows[i].size();
+    s->index.insert(s->index.end(), rows[i].begin(), rows[i].end());
+  }
+  return RG_OK;
+}
+
+// ---- GRID::DryRewet, method 2 -----------------------------------------------
+
+static void dry_rewet(rg_sim* s, int* dried, int* wetted) {
+  const double dryLimit = s->p.dry_limit, rewetLimit = s->p.rewet_limit;
+  const int countDown = s->p.countdown;
+  std::vector<char> nmark(s->np), emark(s->ne);
+  for (int n = 0; n < s->np; n++) {
+    nmark[n] = (s->nflag[n] & N_DRY) != 0;
+    s->nflag[n] &= ~N_MARSH;
+    double H = s->S[n] - s->zor[n];
+    if (H < dryLimit) {
+      s->nflag[n] |= N_DRY;
+      s->countdown[n] = countDown;
+    } else {
+      if (s->countdown[n] > 0)
+        s->countdown[n]--;
+      else
+        s->nflag[n] &= ~N_DRY;
+    }
+    s->z[n] = s->zor[n];
+  }
+  for (int e = 0; e < s->ne; e++) {
+    emark[e] = (s->eflag[e] & E_DRY) != 0;
+    s->eflag[e] &= ~(E_DRY | E_MARSH);
+    const int* nd = &s->en[6 * e];
+    int ndry = 0;
+    for (int i = 0; i < 3; i++)
+      if (s->nflag[nd[i]] & N_DRY) ndry++;
+    if (ndry == 3) {
+      s->eflag[e] |= E_DRY;
+    } else if (ndry) {
+      s->eflag[e] |= E_MARSH;
+      for (int i = 0; i < 3; i++)
+        if (s->nflag[nd[i]] & N_DRY) s->nflag[nd[i]] |= N_MARSH;
+    }
+  }
+  for (int n = 0; n < s->np; n++) s->nflag[n] |= N_DRY;
+  for (int e = 0; e < s->ne; e++) {
+    if (s->eflag[e] & E_DRY) continue;
+    const int* nd = &s->en[6 * e];
+    for (int i = 0; i < 6; i++) s->nflag[nd[i]] &= ~N_DRY;
+    for (int i = 0; i < 3; i++) {
+      const int ni = nd[i];
+      if (!(s->nflag[ni] & N_MARSH)) continue;
+      if (nmark[ni] || s->firstDryRew) {
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        double Si;
+        bool mj = (s->nflag[nd[j]] & N_MARSH) != 0, mk = (s->nflag[nd[k]] & N_MARSH) != 0;
+        if (!mj && !mk)
+          Si = (s->S[nd[j]] + s->S[nd[k]]) / 2.0;
+        else if (!mj)
+          Si = s->S[nd[j]];
+        else if (!mk)
+          Si = s->S[nd[k]];
+        else
+          Si = s->S[nd[(i + 2) % 3]];   // all corners marsh cannot happen for a marsh element
+        s->S[ni] = Si;
+        if (s->S[ni] > s->zor[ni] + rewetLimit) s->S[ni] = s->zor[ni] + rewetLimit;
+        if (s->S[ni] < s->zor[ni] + dryLimit) s->z[ni] = s->S[ni] - dryLimit;
+      } else {
+        if (s->S[ni] < s->zor[ni] + dryLimit) s->z[ni] = s->S[ni] - dryLimit;
+      }
+    }
+  }
+  for (int e = 0; e < s->ne; e++) {
+    const int* nd = &s->en[6 * e];
+    for (int i = 3; i < 6; i++) {
+      int l = nd[i - 3], r = nd[(i - 2) % 3];
+      s->S[nd[i]] = 0.5 * (s->S[l] + s->S[r]);
+      s->z[nd[i]] = 0.5 * (s->z[l] + s->z[r]);
+      if ((s->eflag[e] & E_MARSH) && s->z[nd[i]] + dryLimit / 10.0 < s->zor[nd[i]]) s->nflag[nd[i]] |= N_MARSH;
+    }
+  }
+  for (int n = 0; n < s->np; n++) {
+    if (s->nflag[n] & N_DRY) {
+      s->U[n] = s->V[n] = 0.0;
+      s->S[n] = s->z[n] = s->zor[n];
+      s->dUdt[n] = s->dVdt[n] = s->dSdt[n] = 0.0;
+    }
+  }
+  int d = 0, w = 0;
+  for (int e = 0; e < s->ne; e++) {
+    if ((s->eflag[e] & E_DRY) && !emark[e]) d++;
+    if (!(s->eflag[e] & E_DRY) && emark[e]) w++;
+  }
+  *dried = d;
+  *wetted = w;
+}
+
+// ---- device sync helpers ------------------------------------------------------
+
+static rg_status push_state(rg_sim* s) {
+  return rg_set_state(s->ctx, s->U.data(), s->V.data(), s->S.data(), s->dUdt.data(), s->dVdt.data(),
+                      s->dSdt.data(), s->z.data(), nullptr, nullptr);
+}
+
+static rg_status pull_state(rg_sim* s) {
+  rg_status st = rg_get_state(s->ctx, s->U.data(), s->V.data(), s->S.data(), s->z.data());
+  if (st != RG_OK) return st;
+  return rg_get_dt(s->ctx, s->dUdt.data(), s->dVdt.data(), s->dSdt.data());
+}
+
+static rg_status push_boundary(rg_sim* s) {
+  std::vector<int> nf(s->np), bk(s->np);
+  std::vector<double> r4(4 * (size_t)s->np);
+  for (int n = 0; n < s->np; n++) {
+    nf[n] = (int)s->nflag[n];
+    bk[n] = (int)s->bckind[n];
+    getrot(s, n, &r4[4 * (size_t)n]);
+  }
+  return rg_set_boundary(s->ctx, nf.data(), bk.data(), r4.data(), s->niox.data(), s->nioy.data(), s->bcU.data(),
+                         s->bcS.data());
+}
+
+static rg_status push_model(rg_sim* s) {
+  // element list in the order of MODEL::elem
+  const size_t nme = s->melems.size();
+  std::vector<int> enodes(6 * nme, -1), ennd(nme), eflag(nme);
+  std::vector<double> evt(nme);
+  for (size_t e = 0; e < nme; e++) {
+    int me = s->melems[e];
+    if (me >= 0) {
+      for (int i = 0; i < 6; i++) enodes[6 * e + i] = s->en[6 * me + i];
+      ennd[e] = 6;
+      eflag[e] = (int)s->eflag[me];
+      evt[e] = s->en_vt[me];
+    } else {
+      const BElem& b = s->bel[-1 - me];
+      for (int i = 0; i < 3; i++) enodes[6 * e + i] = b.nd[i];
+      ennd[e] = 3;
+      eflag[e] = (int)b.flag;
+      evt[e] = s->en_vt[b.region];
+    }
+  }
+  rg_status st = rg_set_elements(s->ctx, (int)nme, enodes.data(), ennd.data(), eflag.data(), evt.data());
+  if (st != RG_OK) return st;
+  std::vector<int> eq(s->eqno.begin(), s->eqno.end());
+  st = rg_set_pattern(s->ctx, s->neq, s->width.data(), s->index.data(), eq.data());
+  if (st != RG_OK) return st;
+  return rg_set_update_lists(s->ctx, (int)s->mnodes.size(), s->mnodes.data(), s->ne, s->en.data(), s->zor.data());
+}
+
+// MODEL::DoDryRewet (DoDryRew.cpp:50-239) with method 2 on the host state
+static void slip_flow(rg_sim* s) {
+  // GRID::SetSlipFlow (SlipFlow.cpp:42-80)
+  double r[4];
+  for (int n = 0; n < s->np; n++) {
+    if (!(s->nflag[n] & N_ROTAT)) continue;
+    getrot(s, n, r);
+    double Ut = r[0] * s->U[n] + r[2] * s->V[n];
+    s->U[n] = r[0] * Ut;
+    s->V[n] = r[2] * Ut;
+    Ut = r[0] * s->dUdt[n] + r[2] * s->dVdt[n];
+    s->dUdt[n] = r[0] * Ut;
+    s->dVdt[n] = r[2] * Ut;
+  }
+}
+
+static void do_dry_rewet(rg_sim* s, int* del, int* wel) {
+  connection(s, 0);
+  *del = *wel = 0;
+  if (s->p.dryrew_method == 2) dry_rewet(s, del, wel);
+  if (*del + *wel) {
+    initialize(s);
+    set_normal(s);
+    set_rotation(s, nullptr);
+    slip_flow(s);
+  } else {
+    connection(s, E_DRY);
+  }
+  s->firstDryRew = false;
+}
+
+// =============================================================================
+
+extern "C" {
+
+rg_status rg_sim_create(const rg_deck* d, int precision, int device, rg_sim** out) {
+  if (!d || !out || d->np <= 0 || d->ne <= 0 || !d->x || !d->y || !d->z || !d->elem_nodes || !d->elem_mat ||
+      d->nmat <= 0 || !d->mat_n || !d->mat_vt)
+    return RG_ERR_ARG;
+  for (int e = 0; e < 6 * d->ne; e++)
+    if (d->elem_nodes[e] < 0 || d->elem_nodes[e] >= d->np) return RG_ERR_ARG;
+  for (int e = 0; e < d->ne; e++)
+    if (d->elem_mat[e] < 0 || d->elem_mat[e] >= d->nmat) return RG_ERR_ARG;
+  for (int k = 0; k < 3 * d->nseg; k++)
+    if (d->seg_nodes[k] < 0 || d->seg_nodes[k] >= d->np) return RG_ERR_ARG;
+  rg_sim* s = new rg_sim();
+  *out = s;
+  s->prec = precision;
+  s->p = d->params;
+  s->hmin = s->p.dry_limit / 2.0;   // PROJECT::hmin (Project.cpp:1125)
+  s->np = d->np;
+  s->ne = d->ne;
+  s->x.assign(d->x, d->x + d->np);
+  s->y.assign(d->y, d->y + d->np);
+  s->zor.assign(d->z, d->z + d->np);
+  // mid-side bed elevation is the mean of the corners (GRID::InputRegion, Grid.cpp:350-372)
+  for (int e = 0; e < d->ne; e++) {
+    const int* nd = d->elem_nodes + 6 * (size_t)e;
+    for (int i = 3; i < 6; i++) s->zor[nd[i]] = 0.5 * (s->zor[nd[i - 3]] + s->zor[nd[(i - 2) % 3]]);
+  }
+  s->z = s->zor;
+  s->en.assign(d->elem_nodes, d->elem_nodes + 6 * (size_t)d->ne);
+  s->en_n.resize(d->ne);
+  s->en_vt.resize(d->ne);
+  for (int e = 0; e < d->ne; e++) {
+    s->en_n[e] = d->mat_n[d->elem_mat[e]];
+    s->en_vt[e] = d->mat_vt[d->elem_mat[e]];
+  }
+  s->seg_nodes.assign(d->seg_nodes, d->seg_nodes + 3 * (size_t)d->nseg);
+  s->seg_line.assign(d->seg_line, d->seg_line + d->nseg);
+  for (int b = 0; b < d->nbc; b++) {
+    const rg_line_bc& lb = d->bc[b];
+    LineBc l;
+    l.line = lb.line;
+    if (lb.kind == RG_BC_QINLET) {
+      l.kind = B_QINLET;
+      l.t = {0.0};
+      l.Q = {lb.Q[0]};
+      l.S = {lb.S[0]};
+    } else if (lb.kind == RG_BC_QTINLET) {
+      if (lb.npts < 1) return sfail(s, RG_ERR_ARG, "QTINLET needs points");
+      l.kind = B_QTINLET;
+      l.t.assign(lb.t, lb.t + lb.npts);
+      l.Q.assign(lb.Q, lb.Q + lb.npts);
+      l.S.assign(lb.S, lb.S + lb.npts);
+    } else if (lb.kind == RG_BC_OUTLET) {
+      l.kind = B_OUTLET;
+      l.S = {lb.S[0]};
+    } else {
+      return sfail(s, RG_ERR_ARG, "unsupported boundary condition kind");
+    }
+    s->bcl.push_back(l);
+  }
+  const size_t np = d->np;
+  s->eflag.assign(d->ne, E_REGION);
+  s->nflag.assign(np, 0);
+  for (int e = 0; e < d->ne; e++) {
+    for (int i = 0; i < 3; i++) s->nflag[s->en[6 * e + i]] |= N_CORN;
+    for (int i = 3; i < 6; i++) s->nflag[s->en[6 * e + i]] |= N_MIDS;
+  }
+  s->noel.assign(np, 0);
+  s->countdown.assign(np, 0);
+  s->boundList.assign(np, -1);
+  s->bckind.assign(np, 0);
+  s->rot.assign(np, 0);
+  s->has_val.assign(np, 0);
+  for (auto* v : {&s->bnx, &s->bny, &s->niox, &s->nioy, &s->bcU, &s->bcS, &s->U, &s->V, &s->S, &s->dUdt, &s->dVdt,
+                  &s->dSdt, &s->oU, &s->oV, &s->oS, &s->odUdt, &s->odVdt, &s->odSdt, &s->cf})
+    v->assign(np, 0.0);
+  s->eqno.assign(3 * np, -1);
+  // area factors of inclined elements (ArFact.cpp:41-97), from the initial bed
+  s->en_af.resize(d->ne);
+  for (int e = 0; e < d->ne; e++) {
+    const int* nd = &s->en[6 * e];
+    double xx[3], yy[3], zz[3];
+    xx[0] = s->x[nd[0]];
+    yy[0] = s->y[nd[0]];
+    zz[0] = s->zor[nd[0]];
+    for (int i = 1; i < 3; i++) {
+      xx[i] = s->x[nd[i]] - xx[0];
+      yy[i] = s->y[nd[i]] - yy[0];
+      zz[i] = s->zor[nd[i]] - zz[0];
+    }
+    double t1 = yy[1] * zz[2] - yy[2] * zz[1];
+    double t2 = zz[1] * xx[2] - zz[2] * xx[1];
+    double t3 = xx[1] * yy[2] - xx[2] * yy[1];
+    s->en_af[e] = std::sqrt(t1 * t1 + t2 * t2 + t3 * t3) / t3;
+  }
+  if (device == RG_DEVICE_NONE) return RG_OK;   // host model only (no GPU context)
+  // the GPU context holds the mesh; elements are (re)loaded per model change
+  rg_mesh m;
+  std::vector<int> en1(6, 0), nnd1(1, 6), fl1(1, E_REGION);
+  std::vector<double> vt1(1, 0.0);
+  en1 = std::vector<int>(s->en.begin(), s->en.begin() + 6);
+  m.np = d->np;
+  m.x = s->x.data();
+  m.y = s->y.data();
+  m.ne = 1;
+  m.elem_nodes = en1.data();
+  m.elem_nnd = nnd1.data();
+  m.elem_flag = fl1.data();
+  m.elem_vt = vt1.data();
+  m.g = s->p.g;
+  m.hmin = s->hmin;
+  m.vk = s->p.vk;
+  rg_status st = rg_create(&m, precision, device, &s->ctx);
+  if (st != RG_OK) return sfail(s, st, s->ctx ? rg_last_error(s->ctx) : "rg_create failed");
+  st = rg_set_update_lists(s->ctx, 0, nullptr, s->ne, s->en.data(), s->zor.data());
+  if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
+  st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
+  if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
+  return RG_OK;
+}
+
+rg_ctx* rg_sim_context(rg_sim* s) { return s ? s->ctx : nullptr; }
+
+rg_status rg_sim_destroy(rg_sim* s) {
+  if (!s) return RG_OK;
+  if (s->ctx) rg_destroy(s->ctx);
+  delete s;
+  return RG_OK;
+}
+
+const char* rg_sim_last_error(rg_sim* s) {
+  if (!s) return "null simulation";
+  if (!s->err.empty()) return s->err.c_str();
+  return s->ctx ? rg_last_error(s->ctx) : "";
+}
+
+rg_status rg_sim_set_state(rg_sim* s, const double* U, const double* V, const double* S) {
+  if (!s || !U || !V || !S) return RG_ERR_ARG;
+  s->U.assign(U, U + s->np);
+  s->V.assign(V, V + s->np);
+  s->S.assign(S, S + s->np);
+  std::fill(s->dUdt.begin(), s->dUdt.end(), 0.0);
+  std::fill(s->dVdt.begin(), s->dVdt.end(), 0.0);
+  std::fill(s->dSdt.begin(), s->dSdt.end(), 0.0);
+  s->oU = s->U;
+  s->oV = s->V;
+  s->oS = s->S;
+  s->odUdt = s->dUdt;
+  s->odVdt = s->dVdt;
+  s->odSdt = s->dSdt;
+  // model set-up as at the start of PROJECT::Compute (Compute.cpp:170-180)
+  std::fill(s->cf.begin(), s->cf.end(), 0.0);
+  initialize(s);
+  // boundary nodes of the whole grid keep kGridBnd for good (Model.cpp:301-307)
+  for (int n = 0; n < s->np; n++)
+    if (s->nflag[n] & N_BOUND) s->nflag[n] |= N_GRIDBND;
+  init_bcon(s, 0.0);
+  set_location(s);
+  s->have_state = true;
+  s->eqs_init = -1;
+  return RG_OK;
+}
+
+rg_status rg_sim_get_state(rg_sim* s, double* U, double* V, double* S, double* z, int* nflag) {
+  if (!s) return RG_ERR_ARG;
+  if (U) std::copy(s->U.begin(), s->U.end(), U);
+  if (V) std::copy(s->V.begin(), s->V.end(), V);
+  if (S) std::copy(s->S.begin(), s->S.end(), S);
+  if (z) std::copy(s->z.begin(), s->z.end(), z);
+  if (nflag)
+    for (int n = 0; n < s->np; n++) nflag[n] = (int)s->nflag[n];
+  return RG_OK;
+}
+
+rg_status rg_sim_dry_rewet(rg_sim* s, int* dried, int* wetted) {
+  if (!s || !s->have_state) return RG_ERR_ARG;
+  int d = 0, w = 0;
+  do_dry_rewet(s, &d, &w);
+  if (dried) *dried = d;
+  if (wetted) *wetted = w;
+  return RG_OK;
+}
+
+rg_status rg_sim_prepare_iteration(rg_sim* s, double t_bc, const double* cf) {
+  if (!s || !s->have_state) return RG_ERR_ARG;
+  if (cf) s->cf.assign(cf, cf + s->np);
+  init_bcon(s, t_bc);
+  set_location(s);
+  set_normal(s);
+  set_rotation(s, nullptr);
+  if (s->eqs_init != s->model_init) {
+    s->eqs_init = s->model_init;
+    return set_eqno(s);
+  }
+  return RG_OK;
+}
+
+rg_status rg_sim_get_numbering(rg_sim* s, int* neq, int* eqno, int* width, int64_t* nnz) {
+  if (!s) return RG_ERR_ARG;
+  if (neq) *neq = s->neq;
+  if (eqno) std::copy(s->eqno.begin(), s->eqno.end(), eqno);
+  if (width) std::copy(s->width.begin(), s->width.end(), width);
+  if (nnz) *nnz = (int64_t)s->index.size();
+  return RG_OK;
+}
+
+rg_status rg_sim_get_pattern(rg_sim* s, int* index) {
+  if (!s || !index) return RG_ERR_ARG;
+  std::copy(s->index.begin(), s->index.end(), index);
+  return RG_OK;
+}
+
+rg_status rg_sim_get_boundary(rg_sim* s, int* nflag, int* bckind, double* rot4, double* bcU, double* bcS) {
+  if (!s) return RG_ERR_ARG;
+  for (int n = 0; n < s->np; n++) {
+    if (nflag) nflag[n] = (int)s->nflag[n];
+    if (bckind) bckind[n] = (int)s->bckind[n];
+    if (rot4) getrot(s, n, rot4 + 4 * (size_t)n);
+    if (bcU) bcU[n] = s->bcU[n];
+    if (bcS) bcS[n] = s->bcS[n];
+  }
+  return RG_OK;
+}
+
+rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg_step_report* rep) {
+  if (!s || !ctl || !s->have_state || dt <= 0.0) return RG_ERR_ARG;
+  if (!s->ctx) return sfail(s, RG_ERR_ARG, "rg_sim_step: created without a GPU context");
+  auto t0 = std::chrono::steady_clock::now();
+  const bool steady = ctl->steady != 0;
+  const double th = s->p.theta;
+  double rUV, rH;
+  if (steady) {
+    rUV = rH = 0.0;   // relaxation method < 3, stationary (EqsUVS2D.cpp:117-126)
+  } else {
+    rUV = rH = 1.0 / dt / th;
+  }
+  rg_status st = rg_set_relax(s->ctx, rUV, rH);
+  if (st != RG_OK) return st;
+  // Predict (EqsUVS2D.cpp:1101-1178)
+  for (int n = 0; n < s->np; n++) s->dUdt[n] = s->dVdt[n] = s->dSdt[n] = 0.0;
+  for (int n = 0; n < s->np; n++) {
+    if (s->oS[n] < s->zor[n] + s->p.dry_limit) {
+      if (ctl->first_step || (s->nflag[n] & N_DRYPREV)) {
+        s->oU[n] = s->U[n];
+        s->oV[n] = s->V[n];
+        s->oS[n] = s->S[n];
+      }
+      s->odUdt[n] = s->odVdt[n] = s->odSdt[n] = 0.0;
+    }
+  }
+  st = rg_set_old(s->ctx, s->oU.data(), s->oV.data(), s->oS.data(), s->odUdt.data(), s->odVdt.data(),
+                  s->odSdt.data());
+  if (st != RG_OK) return st;
+  bool NRconv = true, DWconv = true;
+  const int DWfreq = s->p.dryrew_freq;
+  int nextDW = 0;
+  int maxit = ctl->max_newton > 0 ? ctl->max_newton : s->p.max_newton;
+  double first_norm = -1.0;
+  int krylov_total = 0, newton = 0, dw_events = 0;
+  bool converged = false;
+  bool state_on_device = false;
+  int status_solve = RG_OK;
+  s->resid_hist.clear();
+  rg_update_opts uo;
+  uo.relax_method = s->p.relax_method;
+  uo.max_delta_uv = s->p.max_delta_uv;
+  uo.max_delta_s = s->p.max_delta_s;
+  uo.max_us = s->p.max_us;
+  uo.dry_limit = s->p.dry_limit;
+  uo.dryrew_method = s->p.dryrew_method;
+  double last_ratio = 1.0;
+  for (int it = 0; it < maxit; it++) {
+    // dry / rewet every DWfreq iterations or when the corrections converged
+    if (s->p.dryrew_method && DWfreq < s->p.max_newton) {
+      if (nextDW >= 0 && (it == nextDW || NRconv)) {
+        nextDW = it + DWfreq;
+        if (state_on_device) {
+          st = pull_state(s);
+          if (st != RG_OK) return st;
+          state_on_device = false;
+        }
+        int del = 0, wel = 0;
+        do_dry_rewet(s, &del, &wel);
+        dw_events++;
+        // dry/rewet has converged when nothing got wet (EqsUVS2D.cpp:210-212)
+        DWconv = (wel == 0);
+        if (nextDW > maxit) {
+          maxit = nextDW;
+          nextDW = -1;
+          DWconv = true;
+        }
+      }
+    }
+    NRconv = true;
+    if (!state_on_device) {
+      st = push_state(s);
+      if (st != RG_OK) return st;
+      state_on_device = true;
+    }
+    // friction (GPU) and boundary data (host) of this iteration
+    st = rg_friction(s->ctx, s->cf.data());
+    if (st != RG_OK) return st;
+    if (!s->bcl.empty()) {
+      // the inlet distribution reads S, z at the inlet nodes: the device copy is current
+      st = rg_get_state(s->ctx, nullptr, nullptr, s->S.data(), s->z.data());
+      if (st != RG_OK) return st;
+    }
+    if (init_bcon(s, t + dt)) {
+      st = rg_set_state(s->ctx, nullptr, nullptr, s->S.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                        nullptr);
+      if (st != RG_OK) return st;
+    }
+    set_location(s);
+    set_normal(s);
+    std::vector<int> zero_uv;
+    set_rotation(s, &zero_uv);
+    if (!zero_uv.empty()) {
+      st = rg_zero_velocity(s->ctx, (int)zero_uv.size(), zero_uv.data());
+      if (st != RG_OK) return st;
+    }
+    if (s->eqs_init != s->model_init) {
+      s->eqs_init = s->model_init;
+      st = set_eqno(s);
+      if (st != RG_OK) return st;
+      st = push_model(s);
+      if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
+      st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
+      if (st != RG_OK) return st;
+    }
+    st = push_boundary(s);
+    if (st != RG_OK) return st;
+    // assemble, scale: ||B_k|| is the Newton residual
+    st = rg_assemble(s->ctx, nullptr, nullptr, nullptr);
+    if (st != RG_OK) return st;
+    double scale = 0.0;
+    st = rg_scale(s->ctx, &scale);
+    if (st != RG_OK) return st;
+    if (first_norm < 0.0) first_norm = scale;
+    s->resid_hist.push_back(scale);
+    last_ratio = first_norm > 0.0 ? scale / first_norm : 0.0;
+    if (ctl->criterion == RG_CRIT_RESIDUAL && it > 0 && last_ratio <= ctl->residual_tol && DWconv) {
+      converged = true;
+      break;
+    }
+    st = rg_ilu0_factor(s->ctx, nullptr, nullptr);
+    if (st != RG_OK) return st;
+    int its = 0;
+    st = rg_bicgstab(s->ctx, s->p.solver_maxiter, s->p.solver_maxdiff, nullptr, &its, nullptr);
+    krylov_total += its;
+    if (st != RG_OK && st != RG_NOT_CONVERGED) return st;
+    if (st == RG_NOT_CONVERGED) status_solve = RG_NOT_CONVERGED;
+    double stats[6];
+    st = rg_newton_update(s->ctx, &uo, stats);
+    if (st != RG_OK) return st;
+    newton++;
+    if (stats[0] > s->p.conv_uv || stats[1] > s->p.conv_uv || stats[2] > s->p.conv_s) NRconv = false;
+    if (!steady) {
+      st = rg_timegrad(s->ctx, dt, th);
+      if (st != RG_OK) return st;
+    }
+    if (ctl->criterion == RG_CRIT_CORRECTION && NRconv && DWconv) {
+      converged = true;
+      break;
+    }
+  }
+  if (state_on_device) {
+    st = pull_state(s);
+    if (st != RG_OK) return st;
+  }
+  // GRID::SetSlipFlow at the end of the step (EqsUVS2D.cpp:1078)
+  slip_flow(s);
+  // end of the time step (Compute.cpp:774-810)
+  for (int n = 0; n < s->np; n++) {
+    if (s->nflag[n] & N_DRY)
+      s->nflag[n] |= N_DRYPREV;
+    else
+      s->nflag[n] &= ~N_DRYPREV;
+    if (s->nflag[n] & N_MARSH)
+      s->nflag[n] |= N_MARSHPREV;
+    else
+      s->nflag[n] &= ~N_MARSHPREV;
+    s->oU[n] = s->U[n];
+    s->oV[n] = s->V[n];
+    s->oS[n] = s->S[n];
+    s->odUdt[n] = s->dUdt[n];
+    s->odVdt[n] = s->dVdt[n];
+    s->odSdt[n] = s->dSdt[n];
+  }
+  for (int e = 0; e < s->ne; e++) {
+    if (s->eflag[e] & E_DRY)
+      s->eflag[e] |= E_DRYPREV;
+    else
+      s->eflag[e] &= ~E_DRYPREV;
+    if (s->eflag[e] & E_MARSH)
+      s->eflag[e] |= E_MARSHPREV;
+    else
+      s->eflag[e] &= ~E_MARSHPREV;
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  if (rep) {
+    rep->newton_iterations = newton;
+    rep->krylov_iterations = krylov_total;
+    rep->converged = converged ? 1 : 0;
+    rep->residual_first = first_norm;
+    rep->residual_ratio = last_ratio;
+    rep->neq = s->neq;
+    rep->dryrew_events = dw_events;
+    rep->wall_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    int nh = (int)std::min<size_t>(s->resid_hist.size(), 64);
+    rep->n_hist = nh;
+    for (int i = 0; i < nh; i++) rep->residual_hist[i] = s->resid_hist[i];
+    int nd = 0;
+    for (int n = 0; n < s->np; n++)
+      if (s->nflag[n] & N_DRY) nd++;
+    rep->dry_nodes = nd;
+    rep->solver_status = status_solve;
+  }
+  return converged ? RG_OK : RG_NOT_CONVERGED;
+}
+
+}  // extern "C"

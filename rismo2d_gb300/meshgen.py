@@ -131,8 +131,8 @@ def meander(nx: int = 1266, ny: int = 79, length: float = 10000.0, amplitude: fl
     mats = [(k + 1, 1.0 / kst[k], vt) for k in range(nbands)]
     elx = x[els[:, :3]].mean(axis=1)
     etype = (np.minimum((elx / length * nbands).astype(np.int32), nbands - 1) + 1).astype(np.int32)
-    S_out = valley[0] * 0.0 + depth_out       # outlet level above the channel bed at x=length
-    S0 = np.maximum(valley + depth_out, z)    # level pool at the outlet stage, dry where higher
+    S_out = depth_out                         # outlet level above the channel bed at x=length
+    S0 = np.maximum(valley + depth_out, z)    # water surface parallel to the valley, dry where the bed is higher
     return Mesh(x=x.astype(np.float64), y=y.astype(np.float64), z=z, elems=els, elem_type=etype,
                 lines={1: inlet, 2: outlet}, S0=S0, U0=np.zeros_like(x), V0=np.zeros_like(x),
                 materials=mats,

@@ -1,0 +1,213 @@
+"""Python front end of the standalone time stepper (include/rg300_sim.h).
+
+`Simulation` mirrors the reference's run of EQS_UVS2D::Execute per time step
+(EqsUVS2D.cpp:71): construct it from a mesh (rismo2d_gb300.meshgen.Mesh or the
+same arrays read from reference decks), set the initial state, call `step`.
+All numerical work happens in librg300.so; this module only marshals arrays.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+
+from . import _lib
+from ._lib import p
+
+RG_BC_QINLET, RG_BC_QTINLET, RG_BC_OUTLET = 1, 2, 3
+RG_CRIT_CORRECTION, RG_CRIT_RESIDUAL = 0, 1
+RG_DEVICE_NONE = -2
+
+
+class LineBc(C.Structure):
+    _fields_ = [("kind", C.c_int), ("line", C.c_int), ("npts", C.c_int), ("t", C.c_void_p),
+                ("Q", C.c_void_p), ("S", C.c_void_p)]
+
+
+class DeckParams(C.Structure):
+    _fields_ = [("g", C.c_double), ("vk", C.c_double), ("dry_limit", C.c_double), ("rewet_limit", C.c_double),
+                ("dryrew_method", C.c_int), ("dryrew_freq", C.c_int), ("countdown", C.c_int),
+                ("relax_method", C.c_int), ("max_delta_uv", C.c_double), ("max_delta_s", C.c_double),
+                ("max_us", C.c_double), ("conv_uv", C.c_double), ("conv_s", C.c_double), ("max_newton", C.c_int),
+                ("solver_maxiter", C.c_int), ("solver_maxdiff", C.c_double), ("theta", C.c_double)]
+
+
+class Deck(C.Structure):
+    _fields_ = [("np", C.c_int), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("ne", C.c_int),
+                ("elem_nodes", C.c_void_p), ("elem_mat", C.c_void_p), ("nmat", C.c_int), ("mat_n", C.c_void_p),
+                ("mat_vt", C.c_void_p), ("nseg", C.c_int), ("seg_nodes", C.c_void_p), ("seg_line", C.c_void_p),
+                ("nbc", C.c_int), ("bc", C.c_void_p), ("params", DeckParams)]
+
+
+class StepCtl(C.Structure):
+    _fields_ = [("steady", C.c_int), ("first_step", C.c_int), ("criterion", C.c_int),
+                ("residual_tol", C.c_double), ("max_newton", C.c_int)]
+
+
+class StepReport(C.Structure):
+    _fields_ = [("newton_iterations", C.c_int), ("krylov_iterations", C.c_int), ("converged", C.c_int),
+                ("neq", C.c_int), ("dryrew_events", C.c_int), ("dry_nodes", C.c_int), ("solver_status", C.c_int),
+                ("n_hist", C.c_int), ("residual_first", C.c_double), ("residual_ratio", C.c_double),
+                ("wall_ms", C.c_double), ("residual_hist", C.c_double * 64)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "residual_hist"}
+        d["residual_hist"] = [self.residual_hist[i] for i in range(self.n_hist)]
+        return d
+
+
+@dataclasses.dataclass
+class Params:
+    """Deck parameters; defaults are the survey decks' $RELAX/$DRYREW/$SOLVER lines."""
+    g: float = 9.81
+    vk: float = 1.78e-6 / (1.0 + 0.0337 * 10.0 + 0.00022 * 100.0)   # Project.cpp:110, 10 degC
+    dry_limit: float = 0.01
+    rewet_limit: float = 0.02
+    dryrew_method: int = 2
+    dryrew_freq: int = 10
+    countdown: int = 5
+    relax_method: int = 2
+    max_delta_uv: float = 0.5
+    max_delta_s: float = 0.5
+    max_us: float = 100.0
+    conv_uv: float = 1.0e-9
+    conv_s: float = 1.0e-9
+    max_newton: int = 60
+    solver_maxiter: int = 1000
+    solver_maxdiff: float = 1.0e-8
+    theta: float = 1.0
+
+
+class Simulation:
+    """A mesh, its boundary conditions and the GPU state of one run."""
+
+    def __init__(self, mesh, params: Params | None = None, hydrograph=None, precision: int = _lib.PREC_FP64,
+                 device: int = 0):
+        self.lib = _lib.load()
+        self.lib.rg_sim_last_error.restype = C.c_char_p
+        self.params = params or Params()
+        self.mesh = mesh
+        m = mesh
+        mats = sorted(m.materials)
+        mat_index = {no: i for i, (no, _n, _vt) in enumerate(mats)}
+        self._arr = dict(
+            x=np.ascontiguousarray(m.x, np.float64), y=np.ascontiguousarray(m.y, np.float64),
+            z=np.ascontiguousarray(m.z, np.float64),
+            en=np.ascontiguousarray(m.elems, np.int32).reshape(-1),
+            emat=np.ascontiguousarray([mat_index[int(t)] for t in m.elem_type], np.int32),
+            mat_n=np.ascontiguousarray([n for _no, n, _vt in mats], np.float64),
+            mat_vt=np.ascontiguousarray([vt for _no, _n, vt in mats], np.float64))
+        segs, lines = [], []
+        for no, seg in sorted(m.lines.items()):
+            for s in seg:
+                segs.append(s)
+                lines.append(no)
+        self._arr["segs"] = np.ascontiguousarray(np.asarray(segs, np.int32).reshape(-1))
+        self._arr["lines"] = np.ascontiguousarray(lines, np.int32)
+        bcs = []
+        S_in = m.meta.get("S_in", m.meta["S_out"])
+        if hydrograph is None:
+            self._arr["q_t"] = np.array([0.0])
+            self._arr["q_Q"] = np.array([float(m.meta["Q"])])
+            self._arr["q_S"] = np.array([float(S_in)])
+            bcs.append(LineBc(RG_BC_QINLET, 1, 1, p(self._arr["q_t"]), p(self._arr["q_Q"]), p(self._arr["q_S"])))
+        else:
+            h = np.asarray(hydrograph, np.float64)
+            self._arr["q_t"] = np.ascontiguousarray(h[:, 0])
+            self._arr["q_Q"] = np.ascontiguousarray(h[:, 1])
+            self._arr["q_S"] = np.ascontiguousarray(h[:, 2])
+            bcs.append(LineBc(RG_BC_QTINLET, 1, len(h), p(self._arr["q_t"]), p(self._arr["q_Q"]),
+                              p(self._arr["q_S"])))
+        self._arr["o_S"] = np.array([float(m.meta["S_out"])])
+        bcs.append(LineBc(RG_BC_OUTLET, 2, 1, None, None, p(self._arr["o_S"])))
+        self._bcs = (LineBc * len(bcs))(*bcs)
+        pp = self.params
+        dp = DeckParams(pp.g, pp.vk, pp.dry_limit, pp.rewet_limit, pp.dryrew_method, pp.dryrew_freq, pp.countdown,
+                        pp.relax_method, pp.max_delta_uv, pp.max_delta_s, pp.max_us, pp.conv_uv, pp.conv_s,
+                        pp.max_newton, pp.solver_maxiter, pp.solver_maxdiff, pp.theta)
+        a = self._arr
+        self._deck = Deck(len(a["x"]), p(a["x"]), p(a["y"]), p(a["z"]), len(a["emat"]), p(a["en"]), p(a["emat"]),
+                          len(a["mat_n"]), p(a["mat_n"]), p(a["mat_vt"]), len(a["lines"]), p(a["segs"]),
+                          p(a["lines"]), len(bcs), C.cast(self._bcs, C.c_void_p), dp)
+        self.ptr = C.c_void_p()
+        st = self.lib.rg_sim_create(C.byref(self._deck), C.c_int(precision), C.c_int(device), C.byref(self.ptr))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_create: " + self._err())
+        self.np = len(a["x"])
+        self.precision = precision
+        self.step_no = 0
+
+    def _err(self) -> str:
+        if not self.ptr:
+            return ""
+        e = self.lib.rg_sim_last_error(self.ptr)
+        return e.decode() if e else ""
+
+    def close(self):
+        if self.ptr:
+            self.lib.rg_sim_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, U, V, S):
+        U, V, S = (np.ascontiguousarray(v, np.float64) for v in (U, V, S))
+        st = self.lib.rg_sim_set_state(self.ptr, p(U), p(V), p(S))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_set_state: " + self._err())
+        self.step_no = 0
+
+    def get_state(self) -> dict:
+        out = {k: np.zeros(self.np) for k in ("U", "V", "S", "z")}
+        flags = np.zeros(self.np, np.int32)
+        self.lib.rg_sim_get_state(self.ptr, p(out["U"]), p(out["V"]), p(out["S"]), p(out["z"]), p(flags))
+        out["flag"] = flags
+        return out
+
+    def step(self, t: float, dt: float, steady: bool = False, criterion: int = RG_CRIT_RESIDUAL,
+             residual_tol: float = 1e-8, max_newton: int = 0) -> dict:
+        ctl = StepCtl(1 if steady else 0, 1 if self.step_no == 0 else 0, criterion, residual_tol, max_newton)
+        rep = StepReport()
+        st = self.lib.rg_sim_step(self.ptr, C.c_double(t), C.c_double(dt), C.byref(ctl), C.byref(rep))
+        if st not in (_lib.RG_OK, _lib.RG_NOT_CONVERGED):
+            raise _lib.RgError(st, "rg_sim_step: " + self._err())
+        self.step_no += 1
+        return rep.as_dict()
+
+    # -- inspection of the host model (numbering, pattern, boundary data) ----
+    def prepare_iteration(self, t_bc: float, cf=None):
+        cf = None if cf is None else np.ascontiguousarray(cf, np.float64)
+        st = self.lib.rg_sim_prepare_iteration(self.ptr, C.c_double(t_bc), p(cf))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_prepare_iteration: " + self._err())
+
+    def dry_rewet_pass(self):
+        d, w = C.c_int(), C.c_int()
+        st = self.lib.rg_sim_dry_rewet(self.ptr, C.byref(d), C.byref(w))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_dry_rewet: " + self._err())
+        return d.value, w.value
+
+    def numbering(self) -> dict:
+        neq = C.c_int()
+        nnz = C.c_int64()
+        self.lib.rg_sim_get_numbering(self.ptr, C.byref(neq), None, None, C.byref(nnz))
+        eqno = np.zeros(3 * self.np, np.int32)
+        width = np.zeros(neq.value, np.int32)
+        self.lib.rg_sim_get_numbering(self.ptr, None, p(eqno), p(width), None)
+        index = np.zeros(nnz.value, np.int32)
+        self.lib.rg_sim_get_pattern(self.ptr, p(index))
+        return dict(neq=neq.value, eqno=eqno.reshape(-1, 3), width=width, index=index)
+
+    def boundary(self) -> dict:
+        out = dict(nflag=np.zeros(self.np, np.int32), bckind=np.zeros(self.np, np.int32),
+                   rot4=np.zeros((self.np, 4)), bcU=np.zeros(self.np), bcS=np.zeros(self.np))
+        self.lib.rg_sim_get_boundary(self.ptr, p(out["nflag"]), p(out["bckind"]), p(out["rot4"]), p(out["bcU"]),
+                                     p(out["bcS"]))
+        return out

@@ -60,6 +60,14 @@ def run_reference(mesh, workdir: str, refsrc: str, **deck_kw) -> list:
     return refdump.newton_iterations(refdump.read_dump(os.path.join(workdir, "dump.bin")))
 
 
+MEANDER_TINY = dict(nx=32, ny=10, length=800.0, nbands=4, seed=2, depth_out=3.5)
+
+
+def meander_hydrograph():
+    """Q(t) = 300 + 500 sin^2(pi t / 7200) sampled every 600 s, inlet level 4 m."""
+    return [(t, 300.0 + 500.0 * np.sin(np.pi * t / 7200.0) ** 2, 4.0) for t in np.arange(0.0, 7201.0, 600.0)]
+
+
 def pack(its: list, keep: list) -> dict:
     out = {}
     newton = [it for it in its if "state" in it]
@@ -72,7 +80,10 @@ def pack(its: list, keep: list) -> dict:
     out["crs_index"] = c0["index"].astype(np.int32)
     for k in keep:
         it = newton[k]
-        assert np.array_equal(it["crs"]["index"], c0["index"])
+        if not np.array_equal(it["crs"]["index"], c0["index"]):
+            # the wet model changed (dry/rewet): keep this iteration's own pattern
+            out[f"it{k}_crs_width"] = it["crs"]["width"].astype(np.int32)
+            out[f"it{k}_crs_index"] = it["crs"]["index"].astype(np.int32)
         for key in STATE_KEYS:
             out[f"it{k}_{key}"] = np.asarray(it["state"][key])
         out[f"it{k}_A"] = it["crs"]["A"]
@@ -80,6 +91,20 @@ def pack(its: list, keep: list) -> dict:
         out[f"it{k}_X"] = it["x"]["X"]
     for key in STATE_KEYS:
         out[f"final_{key}"] = np.asarray(finals[-1][key])
+    # end-of-step states of every time step (U, V, S, z and the node flags)
+    out["n_steps"] = np.int32(len(finals))
+    for i, f in enumerate(finals):
+        for key in ("U", "V", "S", "z", "flag", "dUdt", "dVdt", "dSdt"):
+            out[f"step{i}_{key}"] = np.asarray(f[key])
+    # Newton iterations per time step
+    per_step, cnt = [], 0
+    for it in its:
+        if "state" in it:
+            cnt += 1
+        elif "final" in it:
+            per_step.append(cnt)
+            cnt = 0
+    out["newton_per_step"] = np.array(per_step, np.int32)
     out["keep"] = np.array(keep, np.int32)
     return out
 
@@ -99,6 +124,12 @@ def main():
         its = run_reference(m, os.path.join(tmp, "cfg1"), args.reference)
         n = len([i for i in its if "state" in i])
         np.savez_compressed(os.path.join(HERE, "channel_1000.npz"), **pack(its, [0, n - 2]))
+        # unsteady meander with flood plains that dry and rewet: three 10 s steps
+        m = meshgen.meander(**MEANDER_TINY)
+        its = run_reference(m, os.path.join(tmp, "meander"), args.reference, steady=False, dt=10.0,
+                            nsteps=3, hydrograph=meander_hydrograph(), maxiter=40)
+        n = len([i for i in its if "state" in i])
+        np.savez_compressed(os.path.join(HERE, "meander_tiny.npz"), **pack(its, [0, 1, n - 1]))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

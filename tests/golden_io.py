@@ -18,17 +18,18 @@ def load(name: str) -> dict:
 def state(g: dict, it) -> dict:
     pre = f"it{it}_" if it != "final" else "final_"
     out = {k[len(pre):]: v for k, v in g.items() if k.startswith(pre)}
-    width = g["crs_width"]
+    width = out.pop("crs_width", g["crs_width"])
     out["width"] = width
-    out["index"] = g["crs_index"]
+    out["index"] = out.pop("crs_index", g["crs_index"])
     ptr = np.zeros(len(width) + 1, np.int64)
     ptr[1:] = np.cumsum(width)
     out["ptr"] = ptr
     out["eqno"] = np.stack([out["eq0"], out["eq1"], out["eq2"]], axis=1).astype(np.int32)
     out["rot4"] = np.stack([out["r00"], out["r01"], out["r10"], out["r11"]], axis=1)
     mats = out["materials"]
-    out["elem_vt"] = mats[:, 3][np.clip(out["elem_type"], 0, len(mats) - 1)]
-    out["region_n"] = mats[:, 2][np.clip(out["region_type"], 0, len(mats) - 1)]
+    # element types are 1-based TYPE ids (TYPE::Getid(i + 1), Type.cpp:409)
+    out["elem_vt"] = mats[:, 3][np.clip(out["elem_type"] - 1, 0, len(mats) - 1)]
+    out["region_n"] = mats[:, 2][np.clip(out["region_type"] - 1, 0, len(mats) - 1)]
     return out
 
 

@@ -10,8 +10,11 @@ REPO = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 
 
 def header_functions():
-    text = open(os.path.join(REPO, "include", "rg300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:rg_status|const char\*)\s+(rg_\w+)\s*\(", text, re.M)))
+    names = set()
+    for h in ("rg300.h", "rg300_sim.h"):
+        text = open(os.path.join(REPO, "include", h)).read()
+        names |= set(re.findall(r"^\s*(?:rg_status|const char\*|rg_ctx\*)\s+(rg_\w+)\s*\(", text, re.M))
+    return sorted(names)
 
 
 def test_header_lists_entry_points():

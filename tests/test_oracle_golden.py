@@ -105,3 +105,19 @@ def test_zero_pivot_repair_runs():
     rc, ILU = oracle.ilu0_factor(ptr, idx, A)
     assert rc == 0
     assert abs(ILU[ptr[5]]) > 1e-20
+
+
+def test_meander_assembly_and_solve_bit_exact():
+    """Unsteady meander with dry flood plains: the oracle reproduces the
+    reference's assembled system and correction at the kept iterations."""
+    g = golden_io.load("meander_tiny.npz")
+    for k in [int(v) for v in g["keep"]]:
+        st = golden_io.state(g, k)
+        m = golden_io.oracle_model(st)
+        A, B = oracle.assemble(m, st["ptr"], st["index"], np.float32)
+        assert np.array_equal(A, st["A"]) and np.array_equal(B, st["B"])
+        s = oracle.scale_l2(st["ptr"], A, B)
+        assert s == g["scales"][k]
+        rc, ILU = oracle.ilu0_factor(st["ptr"], st["index"], A)
+        ok, X, its, _ = oracle.bicgstab(st["ptr"], st["index"], A, ILU, B)
+        assert its == g["iters"][k] and np.array_equal(X, st["X"])
