@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 rg_status rg_fail(rg_ctx* c, rg_status s, const char* msg) {
@@ -31,7 +32,7 @@ rg_status rg_cuda(rg_ctx* c, cudaError_t e, const char* where) {
 template <class T>
 static cudaError_t upload(rg_ctx* c, DBuf<T>& d, const T* h, size_t n) {
   cudaError_t e = d.alloc(n);
-  if (e != cudaSuccess || n == 0) return e;
+  if (e != cudaSuccess || n == 0 || !h) return e;
   return cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->st);
 }
 
@@ -46,14 +47,18 @@ static cudaError_t upload_if(rg_ctx* c, DBuf<T>& d, const T* h, size_t n) {
 }
 
 static rg_status check_device_error(rg_ctx* c) {
-  TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
   TRY(cudaStreamSynchronize(c->st));
-  int e = *c->err_host;
+  int e = c->err_host[0];
   if (e == 0) return RG_OK;
-  TRY(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), c->st));
+  char msg[256];
+  snprintf(msg, sizeof msg, "device wait gave up (kernel %d: row %d waited for %d)", c->err_host[1],
+           c->err_host[2], c->err_host[3]);
+  TRY(cudaMemsetAsync(c->dev_err.p, 0, 4 * sizeof(int), c->st));
+  TRY(cudaStreamSynchronize(c->st));
   if (e & 2) return rg_fail(c, RG_ERR_ZERO_PIVOT, "ILU(0) zero pivot without a repair row");
   if (e & 4) return rg_fail(c, RG_ERR_ARG, "CRS row wider than the supported maximum");
-  return rg_fail(c, RG_ERR_DEVICE_WAIT, "a bounded device-side wait ran out");
+  return rg_fail(c, RG_ERR_DEVICE_WAIT, msg);
 }
 
 // =============================================================================
@@ -254,6 +259,7 @@ rg_status rg_create(const rg_mesh* m, int precision, int device, rg_ctx** out) {
   rg_ctx* c = new rg_ctx();
   *out = c;
   c->prec = precision;
+  if (const char* tr = getenv("RG_TRACE")) c->trace = atoi(tr);
   if (device < 0) {
     TRY(cudaGetDevice(&c->device));
   } else {
@@ -267,7 +273,7 @@ rg_status rg_create(const rg_mesh* m, int precision, int device, rg_ctx** out) {
   TRY(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   for (int i = 0; i < 16; i++) TRY(cudaEventCreate(&c->ev[i]));
   TRY(cudaMallocHost((void**)&c->ks_host, sizeof(KrylovScalars)));
-  TRY(cudaMallocHost((void**)&c->err_host, sizeof(int)));
+  TRY(cudaMallocHost((void**)&c->err_host, 4 * sizeof(int)));
   c->np = m->np;
   c->ne = m->ne;
   c->g = m->g;
@@ -297,8 +303,8 @@ rg_status rg_create(const rg_mesh* m, int precision, int device, rg_ctx** out) {
   TRY(cudaMemsetAsync(c->bckind.p, 0, np * sizeof(int), c->st));
   TRY(c->ks.alloc(1));
   TRY(cudaMemsetAsync(c->ks.p, 0, sizeof(KrylovScalars), c->st));
-  TRY(c->dev_err.alloc(1));
-  TRY(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), c->st));
+  TRY(c->dev_err.alloc(4));
+  TRY(cudaMemsetAsync(c->dev_err.p, 0, 4 * sizeof(int), c->st));
   TRY(c->upd.alloc(16));
   TRY(cudaStreamSynchronize(c->st));
   return RG_OK;

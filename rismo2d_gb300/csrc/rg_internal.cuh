@@ -130,7 +130,8 @@ struct rg_ctx {
   double t_ms[8] = {0};
 
   int persist_blocks = 0;    // co-resident blocks for the persistent kernels
-  int depth_L = 0, depth_U = 0, n_colors = 0;   // dependency depth of the triangular solves
+  int depth_L = 0, depth_U = 0, n_colors = 0;
+  int trace = 0;                // RG_TRACE level (diagnostics to stderr)   // dependency depth of the triangular solves
   cudaEvent_t user_ev[8];
   bool user_ev_ready = false;
 };

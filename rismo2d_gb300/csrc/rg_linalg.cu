@@ -25,7 +25,7 @@
 
 namespace {
 
-constexpr long long kSpinLimit = 1ll << 23;   // ~seconds of polling at L2 latency
+constexpr long long kSpinLimit = 1ll << 20;   // ~0.5 s of polling at L2 latency
 constexpr int kDevErrWait = 1;
 constexpr int kDevErrPivot = 2;
 constexpr int kDevErrWidth = 4;
@@ -64,18 +64,49 @@ template <class T> __device__ __forceinline__ T sentinel();
 template <> __device__ __forceinline__ double sentinel<double>() { return __longlong_as_double((long long)sent64()); }
 template <> __device__ __forceinline__ float sentinel<float>() { return __uint_as_float(sent32()); }
 
+__device__ __forceinline__ int ld_relaxed_i(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// err[0] error bits (any bit set aborts every waiting warp), err[1] kernel
+// tag, err[2] row that gave up, err[3] the dependency it waited for
+__device__ void record_wait_failure(int* err, int tag, int row, int dep) {
+  if (atomicCAS(&err[1], 0, tag) == 0) {
+    err[2] = row;
+    err[3] = dep;
+  }
+  atomicOr(&err[0], kDevErrWait);
+}
+
 template <class T>
-__device__ __forceinline__ T wait_value(const T* p, int* err) {
+__device__ __forceinline__ T wait_value(const T* p, int* err, int tag, int row, int dep) {
   T v = ld_relaxed(p);
   long long it = 0;
   while (is_sent(v)) {
-    if (++it > kSpinLimit) {
-      atomicOr(err, kDevErrWait);
+    ++it;
+    if ((it & 1023) == 0 && ld_relaxed_i(err) != 0) return (T)0;   // another warp gave up
+    if (it > kSpinLimit) {
+      record_wait_failure(err, tag, row, dep);
       return (T)0;
     }
     v = ld_relaxed(p);
   }
   return v;
+}
+
+__device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err, int tag, int row, int dep) {
+  long long it = 0;
+  while (ld_acquire(flag) != epoch) {
+    ++it;
+    if ((it & 1023) == 0 && ld_relaxed_i(err) != 0) return false;
+    if (it > kSpinLimit) {
+      record_wait_failure(err, tag, row, dep);
+      return false;
+    }
+  }
+  return true;
 }
 
 // round-to-nearest products/sums without contraction (keeps the reference's
@@ -170,17 +201,26 @@ __global__ void k_spmv(int n, const int* __restrict__ rowptr, const int* __restr
   if (ks && ks->conv != 0) return;
   constexpr int NDX = (ND > 0) ? ND : 1;
   const int sub = threadIdx.x & 15;
-  const int rows_per_block = blockDim.x >> 4;
+  const int half = (threadIdx.x >> 4) & 1;
   double dv[NDX];
 #pragma unroll
   for (int k = 0; k < NDX; k++) dv[k] = 0.0;
-  for (int row = blockIdx.x * rows_per_block + (threadIdx.x >> 4); row < n; row += gridDim.x * rows_per_block) {
-    const int b = rowptr[row], e = rowptr[row + 1];
+  // two rows per warp; the trip count is uniform across the warp so the
+  // full-mask shuffles below always see all 32 lanes
+  const int warps_per_block = blockDim.x >> 5;
+  const int gwarp = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int nwarp = gridDim.x * warps_per_block;
+  for (int r0 = 2 * gwarp; r0 < n; r0 += 2 * nwarp) {
+    const int row = r0 + half;
+    const bool valid = row < n;
     AT acc = 0;
-    for (int q = b + sub; q < e; q += 16) acc += (AT)A[q] * (AT)x[col[q]];
+    if (valid) {
+      const int b = rowptr[row], e = rowptr[row + 1];
+      for (int q = b + sub; q < e; q += 16) acc += (AT)A[q] * (AT)x[col[q]];
+    }
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (sub == 0) {
+    if (valid && sub == 0) {
       VT rv = (VT)acc;
       r[row] = rv;
       if (ND >= 1) dv[0] += (double)rv * (double)d1[row];
@@ -213,15 +253,7 @@ __device__ void partial_row(int c, int upto, const int* rowptr, const int* col, 
     const int p = lsort_pos[q];
     const int k = rb.col[p];
     if (k >= upto) break;   // sorted by column
-    if (lane == 0) {
-      long long it = 0;
-      while (ld_acquire(&fflag[k]) != epoch) {
-        if (++it > kSpinLimit) {
-          atomicOr(err, kDevErrWait);
-          break;
-        }
-      }
-    }
+    if (lane == 0) wait_flag(&fflag[k], epoch, err, 2, c, k);
     __syncwarp();
     const MT piv = __ldcg(&LU[rowptr[k]]);
     const MT factor = -rb.val[p] / piv;
@@ -256,7 +288,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor(int n, const int* __restr
     const int b = rowptr[i], w = rowptr[i + 1] - b;
     if (w > RG_MAXW) {
       if (lane == 0) {
-        atomicOr(err, kDevErrWidth);
+        atomicOr(&err[0], kDevErrWidth);
         st_release(&fflag[i], epoch);
       }
       continue;
@@ -270,15 +302,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor(int n, const int* __restr
     for (int q = lsort_ptr[i]; q < lsort_ptr[i + 1]; q++) {
       const int p = lsort_pos[q];
       const int k = s.col[p];
-      if (lane == 0) {
-        long long it = 0;
-        while (ld_acquire(&fflag[k]) != epoch) {
-          if (++it > kSpinLimit) {
-            atomicOr(err, kDevErrWait);
-            break;
-          }
-        }
-      }
+      if (lane == 0) wait_flag(&fflag[k], epoch, err, 1, i, k);
       __syncwarp();
       const MT piv = __ldcg(&LU[rowptr[k]]);
       const MT factor = -s.val[p] / piv;
@@ -331,7 +355,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor(int n, const int* __restr
           for (int k = 0; k < wp; k++)
             if (s.col[j] == best[wib].col[k]) s.val[j] = s.val[j] + best[wib].val[k];
       } else if (lane == 0) {
-        atomicOr(err, kDevErrPivot);
+        atomicOr(&err[0], kDevErrPivot);
       }
       __syncwarp();
     }
@@ -369,7 +393,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_trsv(int n, const int* __restric
     VT acc = 0;
     for (int q = beg + lane; q < end; q += 32) {
       const int c = col[q];
-      const VT xv = wait_value<VT>(&x[c], err);
+      const VT xv = wait_value<VT>(&x[c], err, LOWER ? 3 : 4, row, c);
       acc += (VT)val[q] * xv;
     }
     acc = warp_sum(acc);
@@ -730,6 +754,13 @@ static rg_status bicgstab_t(rg_ctx* c, const MT* A, const MT* Lv, const MT* Uv, 
     CK(cudaMemcpyAsync(c->ks_host, ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     it = c->ks_host->it;
+    if (c->trace >= 3) {
+      int eh[4];
+      CK(cudaMemcpy(eh, c->dev_err.p, sizeof(eh), cudaMemcpyDeviceToHost));
+      fprintf(stderr, "[rg]     bicg it=%d diff=%.3e t1=%.3e rho=%.3e alfa=%.3e omega=%.3e conv=%d err=%d/%d/%d/%d\n",
+              it, c->ks_host->diff, c->ks_host->t1, c->ks_host->rho, c->ks_host->alfa, c->ks_host->omega,
+              c->ks_host->conv, eh[0], eh[1], eh[2], eh[3]);
+    }
     if (c->ks_host->conv == 1) break;
     if (c->ks_host->conv == -1) {
       CK(cudaMemcpyAsync(x, xm, n * sizeof(VT), cudaMemcpyDeviceToDevice, c->st));

@@ -26,6 +26,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -996,6 +998,12 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
   uo.dry_limit = s->p.dry_limit;
   uo.dryrew_method = s->p.dryrew_method;
   double last_ratio = 1.0;
+  const bool trace = getenv("RG_TRACE") != nullptr;
+  const bool trace2 = trace && getenv("RG_TRACE")[0] == '2';
+#define STAGE(name)                                          \
+  do {                                                       \
+    if (trace2) fprintf(stderr, "[rg]   stage %s\n", name); \
+  } while (0)
   for (int it = 0; it < maxit; it++) {
     // dry / rewet every DWfreq iterations or when the corrections converged
     if (s->p.dryrew_method && DWfreq < s->p.max_newton) {
@@ -1007,7 +1015,9 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
           state_on_device = false;
         }
         int del = 0, wel = 0;
+        STAGE("dry_rewet");
         do_dry_rewet(s, &del, &wel);
+        if (trace2) fprintf(stderr, "[rg]   dried %d wetted %d\n", del, wel);
         dw_events++;
         // dry/rewet has converged when nothing got wet (EqsUVS2D.cpp:210-212)
         DWconv = (wel == 0);
@@ -1025,6 +1035,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       state_on_device = true;
     }
     // friction (GPU) and boundary data (host) of this iteration
+    STAGE("friction");
     st = rg_friction(s->ctx, s->cf.data());
     if (st != RG_OK) return st;
     if (!s->bcl.empty()) {
@@ -1032,6 +1043,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       st = rg_get_state(s->ctx, nullptr, nullptr, s->S.data(), s->z.data());
       if (st != RG_OK) return st;
     }
+    STAGE("init_bcon");
     if (init_bcon(s, t + dt)) {
       st = rg_set_state(s->ctx, nullptr, nullptr, s->S.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
                         nullptr);
@@ -1047,8 +1059,10 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     }
     if (s->eqs_init != s->model_init) {
       s->eqs_init = s->model_init;
+      STAGE("set_eqno");
       st = set_eqno(s);
       if (st != RG_OK) return st;
+      STAGE("push_model");
       st = push_model(s);
       if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
       st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
@@ -1057,6 +1071,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     st = push_boundary(s);
     if (st != RG_OK) return st;
     // assemble, scale: ||B_k|| is the Newton residual
+    STAGE("assemble");
     st = rg_assemble(s->ctx, nullptr, nullptr, nullptr);
     if (st != RG_OK) return st;
     double scale = 0.0;
@@ -1069,17 +1084,23 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       converged = true;
       break;
     }
+    STAGE("factor");
     st = rg_ilu0_factor(s->ctx, nullptr, nullptr);
     if (st != RG_OK) return st;
+    STAGE("bicgstab");
     int its = 0;
     st = rg_bicgstab(s->ctx, s->p.solver_maxiter, s->p.solver_maxdiff, nullptr, &its, nullptr);
     krylov_total += its;
     if (st != RG_OK && st != RG_NOT_CONVERGED) return st;
     if (st == RG_NOT_CONVERGED) status_solve = RG_NOT_CONVERGED;
     double stats[6];
+    STAGE("update");
     st = rg_newton_update(s->ctx, &uo, stats);
     if (st != RG_OK) return st;
     newton++;
+    if (trace)
+      fprintf(stderr, "[rg] t=%g it=%d neq=%d |B|=%.6e krylov=%d st=%d dU=%.3e dV=%.3e dS=%.3e dw=%d\n", t, it, s->neq,
+              scale, its, (int)st, stats[0], stats[1], stats[2], dw_events);
     if (stats[0] > s->p.conv_uv || stats[1] > s->p.conv_uv || stats[2] > s->p.conv_s) NRconv = false;
     if (!steady) {
       st = rg_timegrad(s->ctx, dt, th);

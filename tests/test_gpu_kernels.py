@@ -147,3 +147,54 @@ def test_friction_matches_reference():
     cf = ctx.friction()
     assert np.max(np.abs(cf - st["cf"])) <= 1e-14 * np.max(np.abs(st["cf"]))
     ctx.close()
+
+
+def _random_system(n, seed):
+    """Structurally symmetric, diagonally dominant sparse system in the
+    reference's row layout (diagonal first, other columns shuffled)."""
+    rng = np.random.default_rng(seed)
+    cols = [set([i]) for i in range(n)]
+    for i in range(n):
+        for j in rng.integers(0, n, size=min(n, 6)):
+            if j != i and abs(int(j) - i) < 40:
+                cols[i].add(int(j))
+                cols[int(j)].add(i)
+    width, index, A = [], [], []
+    for i in range(n):
+        others = [c for c in cols[i] if c != i]
+        rng.shuffle(others)
+        row = [i] + others
+        width.append(len(row))
+        index.extend(row)
+        A.extend([len(row) * 2.0 + rng.random()] + list(rng.uniform(-1, 1, len(others))))
+    width = np.array(width, np.int32)
+    ptr = np.zeros(n + 1, np.int64)
+    ptr[1:] = np.cumsum(width)
+    return width, np.array(index, np.int32), ptr, np.array(A, np.float32), rng.standard_normal(n)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 257, 1001])
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_ragged_sizes_linear_algebra(n, prec):
+    """Odd and tiny equation counts (a half-filled last warp in every kernel)."""
+    g = golden_io.load("channel_tiny.npz")
+    st = golden_io.state(g, 0)
+    ctx = golden_io.gpu_context(st, prec)
+    width, index, ptr, A, b = _random_system(n, n)
+    ctx.set_pattern(width, index, -np.ones((len(st["x"]), 3), np.int32))
+    A_in = A.astype(np.float64) if prec == 0 else A
+    ctx.load_system(A_in, b)
+    x = np.linspace(-1.0, 1.0, n)
+    r = ctx.spmv(x)
+    r_ref = oracle.spmv(ptr, index, A_in, x)
+    assert np.max(np.abs(r - r_ref)) <= 1e-12 * max(1.0, np.max(np.abs(r_ref)))
+    ctx.ilu0_factor()
+    _, ILU = oracle.ilu0_factor(ptr, index, A_in)
+    y = ctx.ilu0_apply(x)
+    y_ref = oracle.ilu0_solve(ptr, index, ILU, x)
+    assert np.max(np.abs(y - y_ref)) <= 1e-5 * max(1.0, np.max(np.abs(y_ref)))
+    ok, X, its, _ = ctx.bicgstab(500, 1e-8)
+    assert ok
+    res = b - oracle.spmv(ptr, index, A_in, X)
+    assert np.linalg.norm(res) <= 1e-6 * np.linalg.norm(b)
+    ctx.close()
