@@ -172,7 +172,9 @@ rg_status rg_friction(rg_ctx* ctx, double* cf_out);
 rg_status rg_get_timings(rg_ctx* ctx, double* ms, int n);
 
 /* Structure of the resident system: [0] neq, [1] nnz, [2] dependency depth of
- * the L solve, [3] of the U solve, [4] element colours, [5] L entries. */
+ * the L solve, [3] of the U solve, [4] element colours, [5] L entries,
+ * [6] / [7] wavefront chunks of the L / U solve, [8] / [9] their entries whose
+ * source lies outside the shared-memory ring. */
 rg_status rg_get_stats(rg_ctx* ctx, int64_t* out, int n);
 
 /* CUDA events on the context's stream (8 slots), for timing a caller's

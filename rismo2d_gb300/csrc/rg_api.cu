@@ -459,6 +459,54 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
     c->depth_U = du;
     c->n_colors = ncol;
   }
+  // wavefront solve layouts (level-ordered chunk images) and the level
+  // schedule of the factorisation
+  {
+    const int vtb = (c->prec == RG_PREC_MIXED) ? 4 : 8;
+    const int ring = (vtb == 8) ? 8192 : 16384;
+    const int stage_cap = 40960, bstage_cap = 4096;
+    std::vector<int> diag_pos(rowptr.begin(), rowptr.end() - 1);
+    WaveLayout wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, ring, stage_cap, bstage_cap);
+    WaveLayout wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, ring, stage_cap, bstage_cap);
+    for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {
+      WaveLayout& w = *pr.first;
+      WaveDev& d = *pr.second;
+      TRY(upload(c, d.img, w.img_host.data(), std::max<size_t>(w.img_host.size(), 16)));
+      TRY(upload(c, d.chunks, w.chunks.data(), std::max<size_t>(w.chunks.size(), 1)));
+      TRY(upload(c, d.order, w.order.data(), std::max<size_t>(w.order.size(), 1)));
+      TRY(upload(c, d.bidx, w.bidx.data(), std::max<size_t>(w.bidx.size(), 1)));
+      TRY(upload(c, d.ent_src, w.ent_src.data(), std::max<size_t>(w.ent_src.size(), 1)));
+      TRY(upload(c, d.ent_dst, w.ent_dst.data(), std::max<size_t>(w.ent_dst.size(), 1)));
+      TRY(upload(c, d.diag_src, w.diag_src.data(), std::max<size_t>(w.diag_src.size(), 1)));
+      TRY(upload(c, d.diag_dst, w.diag_dst.data(), std::max<size_t>(w.diag_dst.size(), 1)));
+      TRY(d.blev.alloc((size_t)w.blev_len * vtb + 64));
+      d.nchunks = (long long)w.chunks.size();
+      d.nent = (long long)w.ent_src.size();
+      d.ndiag = (long long)w.diag_src.size();
+      d.stage_bytes = stage_cap;
+      d.bstage_bytes = bstage_cap;
+      d.depth = w.depth;
+      d.ring_misses = w.ring_misses;
+      TRY(cudaStreamSynchronize(c->st));   // host images are freed at scope end
+    }
+    // factor schedule: rows grouped by L level (the L solve's level order)
+    std::vector<int> lev(neq, 0), fptr;
+    int nlev = 0;
+    for (int i = 0; i < neq; i++) {
+      int l = 0;
+      for (int q = Lptr[i]; q < Lptr[i + 1]; q++) l = std::max(l, lev[Lcol[q]] + 1);
+      lev[i] = l;
+      nlev = std::max(nlev, l + 1);
+    }
+    fptr.assign(nlev + 1, 0);
+    for (int i = 0; i < neq; i++) fptr[lev[i] + 1]++;
+    for (int l = 0; l < nlev; l++) fptr[l + 1] += fptr[l];
+    std::vector<int> frows(neq), fill(fptr.begin(), fptr.end() - 1);
+    for (int i = 0; i < neq; i++) frows[fill[lev[i]]++] = i;
+    TRY(upload(c, c->flev_ptr, fptr.data(), fptr.size()));
+    TRY(upload(c, c->flev_rows, frows.data(), frows.size()));
+    c->waveL.lev_ptr = fptr;
+  }
   TRY(c->fflag.alloc(neq));
   TRY(cudaMemsetAsync(c->fflag.p, 0, neq * sizeof(int), c->st));
   c->fepoch = 0;
@@ -632,8 +680,21 @@ rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
   if (!c || !c->have_system) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_factor: no system");
   TRY(cudaSetDevice(c->device));
   TRY(cudaEventRecord(c->ev[4], c->st));
-  TRY(launch_factor(c));
+  if (c->use_level_factor) {
+    TRY(launch_factor_level(c));
+    TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    TRY(cudaStreamSynchronize(c->st));
+    if (c->err_host[0] & 16) {
+      // a pivot needs the zero-pivot repair: redo with the dependency-driven kernel
+      TRY(cudaMemsetAsync(c->dev_err.p, 0, 4 * sizeof(int), c->st));
+      TRY(launch_factor(c));
+      c->n_repair_fallbacks++;
+    }
+  } else {
+    TRY(launch_factor(c));
+  }
   TRY(launch_split(c));
+  if (c->use_wave) TRY(launch_wave_pack(c));
   TRY(cudaEventRecord(c->ev[5], c->st));
   rg_status s = check_device_error(c);
   if (s != RG_OK) return s;
@@ -859,8 +920,9 @@ rg_status rg_zero_velocity(rg_ctx* c, int n, const int* nodes) {
 
 rg_status rg_get_stats(rg_ctx* c, int64_t* out, int n) {
   if (!c || !out) return RG_ERR_ARG;
-  int64_t v[6] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n};
-  for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+  int64_t v[10] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n,
+                    c->waveL.nchunks, c->waveU.nchunks, c->waveL.ring_misses, c->waveU.ring_misses};
+  for (int i = 0; i < n && i < 10; i++) out[i] = v[i];
   return RG_OK;
 }
 

@@ -53,12 +53,51 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+// level-ordered chunk layout of one triangular factor (rg_trsv.cu)
+struct WaveChunk {
+  long long img_off;   // byte offset of the chunk image (16-aligned)
+  int img_bytes;       // multiple of 16
+  int nrows;
+  int diag_off;        // byte offset of the diagonal inside the image (U solve)
+  int ent_off;         // byte offset of the entries inside the image
+  int b_off;           // element offset into the level-ordered, padded right-hand side
+  int b_bytes;         // multiple of 16
+  int pos0;            // level-order position of the chunk's first row
+  int pad;
+};
+struct WaveLayout {
+  int n = 0, depth = 0;
+  std::vector<WaveChunk> chunks;
+  std::vector<unsigned char> img_host;
+  long long img_bytes = 0;
+  int blev_len = 0;
+  std::vector<int> order, bidx, ent_src, diag_src;
+  std::vector<long long> ent_dst, diag_dst;
+  long long ring_misses = 0;
+};
+WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
+                             const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
+                             int vt_bytes, int ring, int stage_cap, int bstage_cap);
+
 // per-solve scalars kept on the device (BiCGStab state, reductions)
 struct KrylovScalars {
   double rho, alfa, omega, beta;
   double l2r0, diff, accuracy;
   double t1, t2;
   int it, done, conv, restarts;
+};
+
+struct WaveDev {
+  DBuf<unsigned char> img;
+  DBuf<WaveChunk> chunks;
+  DBuf<int> order, bidx, ent_src, diag_src;
+  DBuf<long long> ent_dst, diag_dst;
+  DBuf<unsigned char> blev;
+  long long nchunks = 0, nent = 0, ndiag = 0;
+  int stage_bytes = 0, bstage_bytes = 0, depth = 0;
+  long long ring_misses = 0;
+  // level schedule of the factorisation (L levels)
+  std::vector<int> lev_ptr;
 };
 
 struct rg_ctx {
@@ -130,6 +169,11 @@ struct rg_ctx {
   double t_ms[8] = {0};
 
   int persist_blocks = 0;    // co-resident blocks for the persistent kernels
+  WaveDev waveL, waveU;      // wavefront triangular solves
+  DBuf<int> flev_ptr, flev_rows;   // level schedule of the factorisation
+  int use_wave = 1;
+  int use_level_factor = 1;
+  int n_repair_fallbacks = 0;
   int depth_L = 0, depth_U = 0, n_colors = 0;
   int trace = 0;                // RG_TRACE level (diagnostics to stderr)   // dependency depth of the triangular solves
   cudaEvent_t user_ev[8];
@@ -147,8 +191,11 @@ cudaError_t launch_friction(rg_ctx* c);
 // linear algebra (rg_linalg.cu)
 cudaError_t launch_scale(rg_ctx* c, double* scale_host);
 cudaError_t launch_factor(rg_ctx* c);
+cudaError_t launch_factor_level(rg_ctx* c);
 cudaError_t launch_split(rg_ctx* c);
 cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r);
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x);
 rg_status   run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, double* acc);
+cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void* y, const KrylovScalars* ks);
+cudaError_t launch_wave_pack(rg_ctx* c);
 cudaError_t launch_update(rg_ctx* c, const rg_update_opts* o, double* stats);

@@ -23,6 +23,8 @@
 
 #include <cstdio>
 
+#include <cooperative_groups.h>
+
 namespace {
 
 constexpr long long kSpinLimit = 1ll << 20;   // ~0.5 s of polling at L2 latency
@@ -366,6 +368,59 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor(int n, const int* __restr
   }
 }
 
+// level-scheduled ILU(0): the rows of one dependency level are eliminated in
+// parallel (warp per row, same arithmetic as k_factor), levels separated by a
+// grid-wide barrier.  A pivot below the repair threshold stops the kernel with
+// a flag; the host then reruns the dependency-driven kernel, which repairs.
+template <class MT, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_factor_level(int nlev, const int* __restrict__ lev_ptr,
+                                                             const int* __restrict__ lev_rows,
+                                                             const int* __restrict__ rowptr,
+                                                             const int* __restrict__ col, const MT* __restrict__ A,
+                                                             MT* LU, const int* __restrict__ lsort_ptr,
+                                                             const int* __restrict__ lsort_pos, int* err) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ RowBuf<MT> rows[WARPS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * WARPS + wib, nw = gridDim.x * WARPS;
+  RowBuf<MT>& s = rows[wib];
+  for (int l = 0; l < nlev; l++) {
+    const int b0 = lev_ptr[l], b1 = lev_ptr[l + 1];
+    for (int idx = b0 + gw; idx < b1; idx += nw) {
+      const int i = lev_rows[idx];
+      const int b = rowptr[i], w = rowptr[i + 1] - b;
+      for (int j = lane; j < w; j += 32) {
+        s.col[j] = col[b + j];
+        s.val[j] = A[b + j];
+      }
+      __syncwarp();
+      for (int q = lsort_ptr[i]; q < lsort_ptr[i + 1]; q++) {
+        const int p = lsort_pos[q];
+        const int k = s.col[p];
+        const MT piv = __ldcg(&LU[rowptr[k]]);
+        const MT factor = -s.val[p] / piv;
+        __syncwarp();
+        if (lane == 0) s.val[p] = factor;
+        for (int q2 = rowptr[k] + 1 + lane; q2 < rowptr[k + 1]; q2 += 32) {
+          const int cc = col[q2];
+          if (cc <= k) continue;
+          for (int ll = 0; ll < w; ll++)
+            if (s.col[ll] == cc) {
+              s.val[ll] = add_rn(s.val[ll], mul_rn(factor, __ldcg(&LU[q2])));
+              break;
+            }
+        }
+        __syncwarp();
+      }
+      if (fabs((double)s.val[0]) < 1.0e-20 && lane == 0) atomicOr(&err[0], 16);   // needs the repair path
+      for (int j = lane; j < w; j += 32) __stcg(&LU[b + j], s.val[j]);
+      __syncwarp();
+    }
+    grid.sync();
+  }
+}
+
 // gather the split triangular operands from the factors
 template <class MT>
 __global__ void k_split(int n, const int* rowptr, const MT* LU, int nl, const int* Lsrc, MT* Lv, int nu,
@@ -636,9 +691,39 @@ static cudaError_t launch_factor_t(rg_ctx* c, const MT* A, MT* LU) {
   return cudaLaunchCooperativeKernel((void*)k_factor<MT, WARPS>, blocks, WARPS * 32, args, 0, c->st);
 }
 
+template <class MT, int WARPS>
+static cudaError_t launch_factor_level_t(rg_ctx* c, const MT* A, MT* LU) {
+  static int per_sm = 0;
+  cudaError_t e;
+  if (per_sm == 0) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_level<MT, WARPS>, WARPS * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+    if (per_sm > 4) per_sm = 4;   // enough warps for a level; fewer blocks make the grid barrier cheaper
+  }
+  int blocks = per_sm * c->num_sms;
+  int nlev = (int)c->waveL.lev_ptr.size() - 1;
+  const int* lp = c->flev_ptr.p;
+  const int* lr = c->flev_rows.p;
+  const int* rp = c->rowptr.p;
+  const int* cl = c->col.p;
+  const int* lsp = c->lsort_ptr.p;
+  const int* lspos = c->lsort_pos.p;
+  int* err = c->dev_err.p;
+  void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &err};
+  return cudaLaunchCooperativeKernel((void*)k_factor_level<MT, WARPS>, blocks, WARPS * 32, args, 0, c->st);
+}
+
 cudaError_t launch_factor(rg_ctx* c) {
   if (c->prec == RG_PREC_FP64) return launch_factor_t<double, 4>(c, c->A64.p, c->LU64.p);
   return launch_factor_t<float, 4>(c, c->A32.p, c->LU32.p);
+}
+
+// level-scheduled factorisation; returns cudaSuccess with err bit 16 set in the
+// device error word when a pivot needs the repair path
+cudaError_t launch_factor_level(rg_ctx* c) {
+  if (c->prec == RG_PREC_FP64) return launch_factor_level_t<double, 8>(c, c->A64.p, c->LU64.p);
+  return launch_factor_level_t<float, 8>(c, c->A32.p, c->LU32.p);
 }
 
 cudaError_t launch_split(rg_ctx* c) {
@@ -700,6 +785,7 @@ cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r) {
 }
 
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x) {
+  if (c->use_wave && c->prec != RG_PREC_MIXED) return launch_wave_solve(c, true, b, c->tmp.p, x, nullptr);
   int nb = grid_for(c, c->neq, 256);
   k_fill_sentinel<double><<<nb, 256, 0, c->st>>>(c->tmp.p, c->neq);
   k_fill_sentinel<double><<<nb, 256, 0, c->st>>>(x, c->neq);
@@ -738,7 +824,10 @@ static rg_status bicgstab_t(rg_ctx* c, const MT* A, const MT* Lv, const MT* Uv, 
   for (;;) {
     k_bicg_beta<<<1, 1, 0, c->st>>>(ks);
     k_bicg_p<VT><<<nb, 256, 0, c->st>>>(n, pi, ri, vi, ks, w, yi);
-    CK((ilu_apply_t<VT, MT>(c, Lv, Uv, Dv, pi, w, yi, nullptr)));
+    if (c->use_wave)
+      CK(launch_wave_solve(c, sizeof(VT) == 8, pi, w, yi, nullptr));
+    else
+      CK((ilu_apply_t<VT, MT>(c, Lv, Uv, Dv, pi, w, yi, nullptr)));
     spmv_t<VT, MT, AT, 1>(c, A, yi, vi, r0, nbs, nullptr);
     k_bicg_alfa<<<1, 256, 0, c->st>>>(part, nbs, ks);
     k_bicg_r1<VT><<<nb, 256, 0, c->st>>>(n, ri, vi, ks, part);
@@ -746,7 +835,10 @@ static rg_status bicgstab_t(rg_ctx* c, const MT* A, const MT* Lv, const MT* Uv, 
     k_bicg_xm<VT><<<nb, 256, 0, c->st>>>(n, x, yi, xm, x, ks);
     // second half, skipped on the device once converged or out of iterations
     k_fill_sentinel_if<VT><<<nb, 256, 0, c->st>>>(w, zi, n, ks);
-    CK((ilu_apply_t<VT, MT>(c, Lv, Uv, Dv, ri, w, zi, ks)));
+    if (c->use_wave)
+      CK(launch_wave_solve(c, sizeof(VT) == 8, ri, w, zi, ks));
+    else
+      CK((ilu_apply_t<VT, MT>(c, Lv, Uv, Dv, ri, w, zi, ks)));
     spmv_t<VT, MT, AT, 2>(c, A, zi, ti, ri, nbs, ks);
     k_bicg_omega<<<1, 256, 0, c->st>>>(part, nbs, ks);
     k_bicg_x<VT><<<nb, 256, 0, c->st>>>(n, x, yi, zi, ri, ti, r0, ks, part);
