@@ -506,6 +506,16 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
     TRY(upload(c, c->flev_ptr, fptr.data(), fptr.size()));
     TRY(upload(c, c->flev_rows, frows.data(), frows.size()));
     c->waveL.lev_ptr = fptr;
+    // fill map: one short per (sorted L entry, entry of its pivot row)
+    std::vector<long long> foff(lspos.size() + 1, 0);
+    for (int i = 0; i < neq; i++)
+      for (int q = lsp[i]; q < lsp[i + 1]; q++) {
+        const int k = index[rowptr[i] + lspos[q]];
+        foff[q + 1] = foff[q] + (rowptr[k + 1] - rowptr[k] - 1);
+      }
+    TRY(upload(c, c->fmap_off, foff.data(), foff.size()));
+    TRY(c->fmap.alloc((size_t)std::max<long long>(foff.back(), 1)));
+    TRY(launch_build_fmap(c));
   }
   TRY(c->fflag.alloc(neq));
   TRY(cudaMemsetAsync(c->fflag.p, 0, neq * sizeof(int), c->st));
@@ -680,8 +690,10 @@ rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
   if (!c || !c->have_system) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_factor: no system");
   TRY(cudaSetDevice(c->device));
   TRY(cudaEventRecord(c->ev[4], c->st));
+  c->n_factor_calls++;
   if (c->use_level_factor) {
     TRY(launch_factor_level(c));
+    TRY(cudaEventRecord(c->ev[6], c->st));
     TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
     TRY(cudaStreamSynchronize(c->st));
     if (c->err_host[0] & 16) {
@@ -701,6 +713,10 @@ rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]));
   c->t_ms[2] = ms;
+  if (c->use_level_factor) {
+    TRY(cudaEventElapsedTime(&ms, c->ev[4], c->ev[6]));
+    c->t_ms[5] = ms;   // level-scheduled kernel alone
+  }
   c->have_factor = true;
   if (LU32_out || LU64_out) return copy_out_system(c, nullptr, LU32_out, LU64_out, true);
   return RG_OK;
@@ -920,9 +936,10 @@ rg_status rg_zero_velocity(rg_ctx* c, int n, const int* nodes) {
 
 rg_status rg_get_stats(rg_ctx* c, int64_t* out, int n) {
   if (!c || !out) return RG_ERR_ARG;
-  int64_t v[10] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n,
-                    c->waveL.nchunks, c->waveU.nchunks, c->waveL.ring_misses, c->waveU.ring_misses};
-  for (int i = 0; i < n && i < 10; i++) out[i] = v[i];
+  int64_t v[12] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n,
+                    c->waveL.nchunks, c->waveU.nchunks, c->waveL.ring_misses, c->waveU.ring_misses,
+                    c->n_repair_fallbacks, c->n_factor_calls};
+  for (int i = 0; i < n && i < 12; i++) out[i] = v[i];
   return RG_OK;
 }
 

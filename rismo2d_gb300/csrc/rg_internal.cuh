@@ -171,9 +171,11 @@ struct rg_ctx {
   int persist_blocks = 0;    // co-resident blocks for the persistent kernels
   WaveDev waveL, waveU;      // wavefront triangular solves
   DBuf<int> flev_ptr, flev_rows;   // level schedule of the factorisation
+  DBuf<long long> fmap_off;          // per sorted L entry: offset into fmap
+  DBuf<short> fmap;                  // fill map (position in the row, -1 = dropped)
   int use_wave = 1;
   int use_level_factor = 1;
-  int n_repair_fallbacks = 0;
+  int n_repair_fallbacks = 0, n_factor_calls = 0;
   int depth_L = 0, depth_U = 0, n_colors = 0;
   int trace = 0;                // RG_TRACE level (diagnostics to stderr)   // dependency depth of the triangular solves
   cudaEvent_t user_ev[8];
@@ -192,6 +194,7 @@ cudaError_t launch_friction(rg_ctx* c);
 cudaError_t launch_scale(rg_ctx* c, double* scale_host);
 cudaError_t launch_factor(rg_ctx* c);
 cudaError_t launch_factor_level(rg_ctx* c);
+cudaError_t launch_build_fmap(rg_ctx* c);
 cudaError_t launch_split(rg_ctx* c);
 cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r);
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x);

@@ -21,6 +21,7 @@
 
 #include "rg_internal.cuh"
 
+#include <algorithm>
 #include <cstdio>
 
 #include <cooperative_groups.h>
@@ -421,6 +422,122 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level(int nlev, const int
   }
 }
 
+// fill map of the level-scheduled factorisation: for every L entry p of row i
+// (sorted by column k) and every entry t >= 1 of row k, the position of that
+// column in row i, or -1 (the linear searches of Preco_ilu0.cpp:177-184, done
+// once per pattern)
+__global__ void k_build_fmap(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                             const int* __restrict__ lsort_ptr, const int* __restrict__ lsort_pos,
+                             const long long* __restrict__ fmap_off, short* __restrict__ fmap) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw; i < n; i += nw) {
+    const int b = rowptr[i], w = rowptr[i + 1] - b;
+    for (int q = lsort_ptr[i]; q < lsort_ptr[i + 1]; q++) {
+      const int k = col[b + lsort_pos[q]];
+      const int bk = rowptr[k], wk = rowptr[k + 1] - bk;
+      for (int t = 1 + lane; t < wk; t += 32) {
+        const int cc = col[bk + t];
+        short pos = -1;
+        if (cc > k)
+          for (int l = 0; l < w; l++)
+            if (col[b + l] == cc) {
+              pos = (short)l;
+              break;
+            }
+        fmap[fmap_off[q] + (t - 1)] = pos;
+      }
+    }
+  }
+}
+
+// level-scheduled ILU(0) with the fill map: per row, the pivots and pivot rows
+// of all its L entries are fetched in one parallel batch into shared memory,
+// then the eliminations run in column order from shared memory
+template <class MT, int WARPS, int STAGE>
+__global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const int* __restrict__ lev_ptr,
+                                                              const int* __restrict__ lev_rows,
+                                                              const int* __restrict__ rowptr,
+                                                              const int* __restrict__ col,
+                                                              const MT* __restrict__ A, MT* LU,
+                                                              const int* __restrict__ lsort_ptr,
+                                                              const int* __restrict__ lsort_pos,
+                                                              const long long* __restrict__ fmap_off,
+                                                              const short* __restrict__ fmap, int* err) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ MT sval[WARPS][RG_MAXW];
+  __shared__ MT spiv[WARPS][RG_MAXW];
+  __shared__ int sbeg[WARPS][RG_MAXW + 1];     // start of each pivot row in the stage
+  __shared__ MT stage[WARPS][STAGE];
+  __shared__ short smap[WARPS][STAGE];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * WARPS + wib, nw = gridDim.x * WARPS;
+  for (int l = 0; l < nlev; l++) {
+    const int b0 = lev_ptr[l], b1 = lev_ptr[l + 1];
+    for (int idx = b0 + gw; idx < b1; idx += nw) {
+      const int i = lev_rows[idx];
+      const int b = rowptr[i], w = rowptr[i + 1] - b;
+      const int q0 = lsort_ptr[i], nl = lsort_ptr[i + 1] - q0;
+      for (int j = lane; j < w; j += 32) sval[wib][j] = A[b + j];
+      // stage layout: pivot row p occupies [sbeg[p], sbeg[p+1]) (its entries 1..w_k-1)
+      if (lane == 0) {
+        int acc = 0;
+        for (int p = 0; p < nl; p++) {
+          sbeg[wib][p] = acc;
+          const int k = col[b + lsort_pos[q0 + p]];
+          acc += rowptr[k + 1] - rowptr[k] - 1;
+        }
+        sbeg[wib][nl] = acc;
+      }
+      __syncwarp();
+      const bool staged = sbeg[wib][nl] <= STAGE;
+      for (int p = lane; p < nl; p += 32) {
+        const int k = col[b + lsort_pos[q0 + p]];
+        spiv[wib][p] = __ldcg(&LU[rowptr[k]]);
+      }
+      if (staged) {
+        for (int p = 0; p < nl; p++) {
+          const int k = col[b + lsort_pos[q0 + p]];
+          const int bk = rowptr[k] + 1, cnt = rowptr[k + 1] - bk, dst = sbeg[wib][p];
+          const long long mo = fmap_off[q0 + p];
+          for (int t = lane; t < cnt; t += 32) {
+            stage[wib][dst + t] = __ldcg(&LU[bk + t]);
+            smap[wib][dst + t] = fmap[mo + t];
+          }
+        }
+      }
+      __syncwarp();
+      for (int p = 0; p < nl; p++) {
+        const int pp = lsort_pos[q0 + p];
+        const MT factor = -sval[wib][pp] / spiv[wib][p];
+        __syncwarp();
+        if (lane == 0) sval[wib][pp] = factor;
+        const int dst = sbeg[wib][p], cnt = sbeg[wib][p + 1] - dst;
+        if (staged) {
+          for (int t = lane; t < cnt; t += 32) {
+            const int pos = smap[wib][dst + t];
+            if (pos >= 0) sval[wib][pos] = add_rn(sval[wib][pos], mul_rn(factor, stage[wib][dst + t]));
+          }
+        } else {
+          const int k = col[b + pp];
+          const int bk = rowptr[k] + 1;
+          const long long mo = fmap_off[q0 + p];
+          for (int t = lane; t < cnt; t += 32) {
+            const int pos = fmap[mo + t];
+            if (pos >= 0) sval[wib][pos] = add_rn(sval[wib][pos], mul_rn(factor, __ldcg(&LU[bk + t])));
+          }
+        }
+        __syncwarp();
+      }
+      if (lane == 0 && fabs((double)sval[wib][0]) < 1.0e-20) atomicOr(&err[0], 16);   // needs the repair path
+      for (int j = lane; j < w; j += 32) __stcg(&LU[b + j], sval[wib][j]);
+      __syncwarp();
+    }
+    grid.sync();
+  }
+}
+
 // gather the split triangular operands from the factors
 template <class MT>
 __global__ void k_split(int n, const int* rowptr, const MT* LU, int nl, const int* Lsrc, MT* Lv, int nu,
@@ -719,9 +836,46 @@ cudaError_t launch_factor(rg_ctx* c) {
   return launch_factor_t<float, 4>(c, c->A32.p, c->LU32.p);
 }
 
+template <class MT, int WARPS, int STAGE>
+static cudaError_t launch_factor_level2_t(rg_ctx* c, const MT* A, MT* LU) {
+  static int per_sm = 0;
+  cudaError_t e;
+  if (per_sm == 0) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_level2<MT, WARPS, STAGE>, WARPS * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+  }
+  const std::vector<int>& lp_h = c->waveL.lev_ptr;
+  int maxw = 1;
+  for (size_t l = 0; l + 1 < lp_h.size(); l++) maxw = std::max(maxw, lp_h[l + 1] - lp_h[l]);
+  int blocks = std::min(per_sm * c->num_sms, (maxw + WARPS - 1) / WARPS);
+  int nlev = (int)lp_h.size() - 1;
+  const int* lp = c->flev_ptr.p;
+  const int* lr = c->flev_rows.p;
+  const int* rp = c->rowptr.p;
+  const int* cl = c->col.p;
+  const int* lsp = c->lsort_ptr.p;
+  const int* lspos = c->lsort_pos.p;
+  const long long* fo = c->fmap_off.p;
+  const short* fm = c->fmap.p;
+  int* err = c->dev_err.p;
+  void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &fo, &fm, &err};
+  return cudaLaunchCooperativeKernel((void*)k_factor_level2<MT, WARPS, STAGE>, blocks, WARPS * 32, args, 0, c->st);
+}
+
+cudaError_t launch_build_fmap(rg_ctx* c) {
+  k_build_fmap<<<c->num_sms * 4, 256, 0, c->st>>>(c->neq, c->rowptr.p, c->col.p, c->lsort_ptr.p, c->lsort_pos.p,
+                                                   c->fmap_off.p, c->fmap.p);
+  return cudaGetLastError();
+}
+
 // level-scheduled factorisation; returns cudaSuccess with err bit 16 set in the
 // device error word when a pivot needs the repair path
 cudaError_t launch_factor_level(rg_ctx* c) {
+  if (c->fmap.p) {
+    if (c->prec == RG_PREC_FP64) return launch_factor_level2_t<double, 4, 768>(c, c->A64.p, c->LU64.p);
+    return launch_factor_level2_t<float, 4, 1536>(c, c->A32.p, c->LU32.p);
+  }
   if (c->prec == RG_PREC_FP64) return launch_factor_level_t<double, 8>(c, c->A64.p, c->LU64.p);
   return launch_factor_level_t<float, 8>(c, c->A32.p, c->LU32.p);
 }
