@@ -463,11 +463,13 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
   // schedule of the factorisation
   {
     const int vtb = (c->prec == RG_PREC_MIXED) ? 4 : 8;
-    const int ring = (vtb == 8) ? 8192 : 16384;
-    const int stage_cap = 40960, bstage_cap = 4096;
+    const int stage_cap = (vtb == 8) ? kWaveStage64 : kWaveStage32;
+    const int bstage_cap = (vtb == 8) ? kWaveBStage64 : kWaveBStage32;
     std::vector<int> diag_pos(rowptr.begin(), rowptr.end() - 1);
-    WaveLayout wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, ring, stage_cap, bstage_cap);
-    WaveLayout wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, ring, stage_cap, bstage_cap);
+    WaveLayout wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, kWavePin, stage_cap,
+                                      bstage_cap);
+    WaveLayout wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, kWavePin, stage_cap,
+                                      bstage_cap);
     for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {
       WaveLayout& w = *pr.first;
       WaveDev& d = *pr.second;
@@ -514,6 +516,10 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
         foff[q + 1] = foff[q] + (rowptr[k + 1] - rowptr[k] - 1);
       }
     TRY(upload(c, c->fmap_off, foff.data(), foff.size()));
+    std::vector<int> lscol(std::max<size_t>(lspos.size(), 1), 0);
+    for (int i = 0; i < neq; i++)
+      for (int q = lsp[i]; q < lsp[i + 1]; q++) lscol[q] = index[rowptr[i] + lspos[q]];
+    TRY(upload(c, c->lsort_col, lscol.data(), lscol.size()));
     TRY(c->fmap.alloc((size_t)std::max<long long>(foff.back(), 1)));
     TRY(launch_build_fmap(c));
   }

@@ -58,13 +58,21 @@ struct WaveChunk {
   long long img_off;   // byte offset of the chunk image (16-aligned)
   int img_bytes;       // multiple of 16
   int nrows;
-  int diag_off;        // byte offset of the diagonal inside the image (U solve)
-  int ent_off;         // byte offset of the entries inside the image
+  int nent;
+  int diag_off;        // byte offsets inside the image: diagonal (U solve), values, sources
+  int val_off;
+  int src_off;
   int b_off;           // element offset into the level-ordered, padded right-hand side
   int b_bytes;         // multiple of 16
   int pos0;            // level-order position of the chunk's first row
   int pad;
 };
+// shared-memory budget of the wavefront solve (per precision of the vectors):
+// ring and pinned slots, three image stages, three right-hand-side stages
+constexpr int kWaveRing = 16384;
+constexpr int kWavePin = 4096;
+constexpr int kWaveStage32 = 40960, kWaveBStage32 = 4096;   // float: 64+16+120+12 KB
+constexpr int kWaveStage64 = 20480, kWaveBStage64 = 2048;   // double: 128+32+60+6 KB
 struct WaveLayout {
   int n = 0, depth = 0;
   std::vector<WaveChunk> chunks;
@@ -74,10 +82,14 @@ struct WaveLayout {
   std::vector<int> order, bidx, ent_src, diag_src;
   std::vector<long long> ent_dst, diag_dst;
   long long ring_misses = 0;
+  int pinned = 0;
 };
+// ring: shared-memory ring slots; pin: fixed slots for sources read from
+// farther back than the ring reaches (src encoding: [0, ring) ring slot,
+// [ring, ring + pin) pinned slot, negative: -(row + 1) in global memory)
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
                              const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
-                             int vt_bytes, int ring, int stage_cap, int bstage_cap);
+                             int vt_bytes, int ring, int pin, int stage_cap, int bstage_cap);
 
 // per-solve scalars kept on the device (BiCGStab state, reductions)
 struct KrylovScalars {
@@ -172,6 +184,7 @@ struct rg_ctx {
   WaveDev waveL, waveU;      // wavefront triangular solves
   DBuf<int> flev_ptr, flev_rows;   // level schedule of the factorisation
   DBuf<long long> fmap_off;          // per sorted L entry: offset into fmap
+  DBuf<int> lsort_col;               // per sorted L entry: its column (the pivot row)
   DBuf<short> fmap;                  // fill map (position in the row, -1 = dropped)
   int use_wave = 1;
   int use_level_factor = 1;

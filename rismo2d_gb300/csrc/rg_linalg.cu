@@ -462,6 +462,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
                                                               const MT* __restrict__ A, MT* LU,
                                                               const int* __restrict__ lsort_ptr,
                                                               const int* __restrict__ lsort_pos,
+                                                              const int* __restrict__ lsort_col,
                                                               const long long* __restrict__ fmap_off,
                                                               const short* __restrict__ fmap, int* err) {
   namespace cg = cooperative_groups;
@@ -469,6 +470,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
   __shared__ MT sval[WARPS][RG_MAXW];
   __shared__ MT spiv[WARPS][RG_MAXW];
   __shared__ int sbeg[WARPS][RG_MAXW + 1];     // start of each pivot row in the stage
+  __shared__ int spos[WARPS][RG_MAXW];         // position of the L entry in the row
+  __shared__ int srow[WARPS][RG_MAXW];         // first U-side entry of the pivot row
   __shared__ MT stage[WARPS][STAGE];
   __shared__ short smap[WARPS][STAGE];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -480,26 +483,34 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
       const int b = rowptr[i], w = rowptr[i + 1] - b;
       const int q0 = lsort_ptr[i], nl = lsort_ptr[i + 1] - q0;
       for (int j = lane; j < w; j += 32) sval[wib][j] = A[b + j];
-      // stage layout: pivot row p occupies [sbeg[p], sbeg[p+1]) (its entries 1..w_k-1)
-      if (lane == 0) {
-        int acc = 0;
-        for (int p = 0; p < nl; p++) {
-          sbeg[wib][p] = acc;
-          const int k = col[b + lsort_pos[q0 + p]];
-          acc += rowptr[k + 1] - rowptr[k] - 1;
+      // pivot rows of all L entries in one parallel batch; stage offsets by a warp scan
+      int run = 0;
+      for (int p0 = 0; p0 < nl; p0 += 32) {
+        const int p = p0 + lane;
+        int cnt = 0;
+        if (p < nl) {
+          const int k = lsort_col[q0 + p];
+          const int rb = rowptr[k];
+          cnt = rowptr[k + 1] - rb - 1;
+          spiv[wib][p] = __ldcg(&LU[rb]);
+          spos[wib][p] = lsort_pos[q0 + p];
+          srow[wib][p] = rb + 1;
         }
-        sbeg[wib][nl] = acc;
+        int v = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += t;
+        }
+        if (p < nl) sbeg[wib][p] = run + v - cnt;
+        run += __shfl_sync(0xffffffffu, v, 31);
       }
+      if (lane == 0) sbeg[wib][nl] = run;
       __syncwarp();
-      const bool staged = sbeg[wib][nl] <= STAGE;
-      for (int p = lane; p < nl; p += 32) {
-        const int k = col[b + lsort_pos[q0 + p]];
-        spiv[wib][p] = __ldcg(&LU[rowptr[k]]);
-      }
+      const bool staged = run <= STAGE;
       if (staged) {
         for (int p = 0; p < nl; p++) {
-          const int k = col[b + lsort_pos[q0 + p]];
-          const int bk = rowptr[k] + 1, cnt = rowptr[k + 1] - bk, dst = sbeg[wib][p];
+          const int bk = srow[wib][p], dst = sbeg[wib][p], cnt = sbeg[wib][p + 1] - dst;
           const long long mo = fmap_off[q0 + p];
           for (int t = lane; t < cnt; t += 32) {
             stage[wib][dst + t] = __ldcg(&LU[bk + t]);
@@ -509,7 +520,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
       }
       __syncwarp();
       for (int p = 0; p < nl; p++) {
-        const int pp = lsort_pos[q0 + p];
+        const int pp = spos[wib][p];
         const MT factor = -sval[wib][pp] / spiv[wib][p];
         __syncwarp();
         if (lane == 0) sval[wib][pp] = factor;
@@ -520,8 +531,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
             if (pos >= 0) sval[wib][pos] = add_rn(sval[wib][pos], mul_rn(factor, stage[wib][dst + t]));
           }
         } else {
-          const int k = col[b + pp];
-          const int bk = rowptr[k] + 1;
+          const int bk = srow[wib][p];
           const long long mo = fmap_off[q0 + p];
           for (int t = lane; t < cnt; t += 32) {
             const int pos = fmap[mo + t];
@@ -848,7 +858,8 @@ static cudaError_t launch_factor_level2_t(rg_ctx* c, const MT* A, MT* LU) {
   const std::vector<int>& lp_h = c->waveL.lev_ptr;
   int maxw = 1;
   for (size_t l = 0; l + 1 < lp_h.size(); l++) maxw = std::max(maxw, lp_h[l + 1] - lp_h[l]);
-  int blocks = std::min(per_sm * c->num_sms, (maxw + WARPS - 1) / WARPS);
+  // enough warps for a typical level, few enough blocks for a cheap grid barrier
+  int blocks = std::min(std::min(per_sm * c->num_sms, c->num_sms), (maxw + WARPS - 1) / WARPS);
   int nlev = (int)lp_h.size() - 1;
   const int* lp = c->flev_ptr.p;
   const int* lr = c->flev_rows.p;
@@ -856,10 +867,11 @@ static cudaError_t launch_factor_level2_t(rg_ctx* c, const MT* A, MT* LU) {
   const int* cl = c->col.p;
   const int* lsp = c->lsort_ptr.p;
   const int* lspos = c->lsort_pos.p;
+  const int* lscol = c->lsort_col.p;
   const long long* fo = c->fmap_off.p;
   const short* fm = c->fmap.p;
   int* err = c->dev_err.p;
-  void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &fo, &fm, &err};
+  void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &lscol, &fo, &fm, &err};
   return cudaLaunchCooperativeKernel((void*)k_factor_level2<MT, WARPS, STAGE>, blocks, WARPS * 32, args, 0, c->st);
 }
 
@@ -873,8 +885,8 @@ cudaError_t launch_build_fmap(rg_ctx* c) {
 // device error word when a pivot needs the repair path
 cudaError_t launch_factor_level(rg_ctx* c) {
   if (c->fmap.p) {
-    if (c->prec == RG_PREC_FP64) return launch_factor_level2_t<double, 4, 768>(c, c->A64.p, c->LU64.p);
-    return launch_factor_level2_t<float, 4, 1536>(c, c->A32.p, c->LU32.p);
+    if (c->prec == RG_PREC_FP64) return launch_factor_level2_t<double, 4, 640>(c, c->A64.p, c->LU64.p);
+    return launch_factor_level2_t<float, 4, 1280>(c, c->A32.p, c->LU32.p);
   }
   if (c->prec == RG_PREC_FP64) return launch_factor_level_t<double, 8>(c, c->A64.p, c->LU64.p);
   return launch_factor_level_t<float, 8>(c, c->A32.p, c->LU32.p);

@@ -64,25 +64,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-template <class VT>
-struct alignas(8) WEntry;
-template <>
-struct alignas(8) WEntry<float> {
-  float v;
-  int src;
-};
-template <>
-struct alignas(16) WEntry<double> {
-  double v;
-  int src;
-  int pad;
-};
-
 }  // namespace
 
 namespace {
 
-template <class VT, bool LOWER, int RING>
+template <class VT, bool LOWER, int RING, int PIN>
 __global__ void __launch_bounds__(kThreads, 1)
     k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, const unsigned char* __restrict__ img,
                 const VT* __restrict__ blev, VT* __restrict__ x, int stage_bytes, int bstage_bytes, int* err,
@@ -90,8 +76,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (ks && ks->conv != 0) return;
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int NST = 3;
-  VT* ring = reinterpret_cast<VT*>(smem);
-  unsigned char* stage0 = smem + RING * sizeof(VT);
+  // solution values: ring slots [0, RING), pinned long-range slots [RING, RING + PIN)
+  VT* vals = reinterpret_cast<VT*>(smem);
+  unsigned char* stage0 = smem + (RING + PIN) * sizeof(VT);
   unsigned char* bstage0 = stage0 + NST * (size_t)stage_bytes;
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
@@ -114,7 +101,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   for (int k = 0; k < nchunks; k++) {
     const int s = k % NST;
     const unsigned parity = (unsigned)((k / NST) & 1);
-    // every thread waits on the stage's barrier (bounded)
     {
       long long it = 0;
       while (!mbar_try_wait(&bars[s], parity)) {
@@ -128,20 +114,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     const unsigned char* st = stage0 + s * (size_t)stage_bytes;
     const int4* meta = reinterpret_cast<const int4*>(st);
     const VT* diag = reinterpret_cast<const VT*>(st + ch.diag_off);
-    const WEntry<VT>* ent = reinterpret_cast<const WEntry<VT>*>(st + ch.ent_off);
+    const VT* ev = reinterpret_cast<const VT*>(st + ch.val_off);
+    const int* es = reinterpret_cast<const int*>(st + ch.src_off);
     const VT* bv = reinterpret_cast<const VT*>(bstage0 + s * (size_t)bstage_bytes);
     const int m = ch.nrows;
     for (int base = 0; base < m; base += rows_per_pass) {   // uniform trip count
       const int r = base + tid / kGroup;
       const bool valid = r < m;
       VT acc = 0;
-      int4 mt = make_int4(0, 0, 0, 0);
+      int4 mt = make_int4(0, 0, 0, -1);
       if (valid) {
         mt = meta[r];
         for (int e = mt.y + g; e < mt.y + mt.z; e += kGroup) {
-          const WEntry<VT> en = ent[e];
-          const VT xv = (en.src >= 0) ? ring[en.src] : x[-en.src - 1];
-          acc += en.v * xv;
+          const int src = es[e];
+          const VT xv = (src >= 0) ? vals[src] : x[-src - 1];
+          acc += ev[e] * xv;
         }
       }
       acc += __shfl_xor_sync(0xffffffffu, acc, 1);
@@ -152,7 +139,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           xi = bv[r] + acc;
         else
           xi = (bv[r] - acc) / diag[r];
-        ring[(ch.pos0 + r) % RING] = xi;
+        vals[(ch.pos0 + r) % RING] = xi;
+        if (mt.w >= 0) vals[mt.w] = xi;
         x[mt.x] = xi;
       }
     }
@@ -191,22 +179,24 @@ __global__ void k_pack_wave(int nent, const long long* __restrict__ ent_dst, con
 
 template <class VT, bool LOWER>
 static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, const KrylovScalars* ks) {
-  constexpr int RING = (sizeof(VT) == 8) ? 8192 : 16384;
+  constexpr int RING = kWaveRing;
+  constexpr int PIN = kWavePin;
   const int n = c->neq;
   int nb = (n + 255) / 256;
   if (nb > c->num_sms * 4) nb = c->num_sms * 4;
   VT* blev = reinterpret_cast<VT*>(wd.blev.p);
   k_gather_lev<VT><<<nb, 256, 0, c->st>>>(n, wd.order.p, wd.bidx.p, b, blev, ks);
-  const size_t smem = RING * sizeof(VT) + 3 * (size_t)wd.stage_bytes + 3 * (size_t)wd.bstage_bytes;
+  const size_t smem = (RING + PIN) * sizeof(VT) + 3 * (size_t)wd.stage_bytes + 3 * (size_t)wd.bstage_bytes;
   static bool attr_done[2][2] = {{false, false}, {false, false}};
   bool& done = attr_done[sizeof(VT) == 8][LOWER];
   cudaError_t e;
   if (!done) {
-    e = cudaFuncSetAttribute(k_trsv_wave<VT, LOWER, RING>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_trsv_wave<VT, LOWER, RING, PIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
     if (e != cudaSuccess) return e;
     done = true;
   }
-  k_trsv_wave<VT, LOWER, RING><<<1, kThreads, smem, c->st>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, blev, x,
+  k_trsv_wave<VT, LOWER, RING, PIN><<<1, kThreads, smem, c->st>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, blev, x,
                                                              wd.stage_bytes, wd.bstage_bytes, c->dev_err.p, ks);
   return cudaGetLastError();
 }

@@ -13,10 +13,10 @@
 // the factor positions of those entries; diag_pos the diagonal positions.
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
                              const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
-                             int vt_bytes, int ring, int stage_cap, int bstage_cap) {
+                             int vt_bytes, int ring, int pin, int stage_cap, int bstage_cap) {
   WaveLayout w;
   w.n = n;
-  // levels
+  // dependency levels, rows of a level in solve order
   std::vector<int> lev(n, 0);
   int nlev = 0;
   for (int t = 0; t < n; t++) {
@@ -32,15 +32,17 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   for (int l = 0; l < nlev; l++) cnt[l + 1] += cnt[l];
   std::vector<int> order(n), pos(n), fill(cnt.begin(), cnt.end() - 1);
   for (int t = 0; t < n; t++) {
-    const int i = lower ? t : n - 1 - t;   // rows of a level in solve order
+    const int i = lower ? t : n - 1 - t;
     const int p = fill[lev[i]]++;
     order[p] = i;
     pos[i] = p;
   }
-  const int ent_bytes = (vt_bytes == 8) ? 16 : 8;
   auto a16 = [](long long v) { return (v + 15) & ~15ll; };
-  // chunks: consecutive rows of a level, within the stage capacities
-  std::vector<int> chunk_of(n);
+  // chunk image: meta[m] (int4) | diag[m] (VT) | vals[ne] (VT) | srcs[ne] (int), each part 16-aligned
+  auto img_size = [&](long long m, long long ne) {
+    return a16(16 * m) + a16(vt_bytes * m) + a16(vt_bytes * ne) + a16(4 * ne);
+  };
+  std::vector<int> chunk_end(n);
   int p = 0;
   long long img_off = 0;
   int b_off = 0;
@@ -54,53 +56,72 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
     while (p + m < lend) {
       const int i = order[p + m];
       const int k = ptr[i + 1] - ptr[i];
-      long long bytes = a16(16ll * (m + 1)) + a16((long long)vt_bytes * (m + 1)) + (long long)ent_bytes * (ne + k);
-      long long bb = a16((long long)vt_bytes * (m + 1));
-      if (m > 0 && (a16(bytes) > stage_cap || bb > bstage_cap || m + 1 > 4096)) break;
+      if (m > 0 && (img_size(m + 1, ne + k) > stage_cap || a16((long long)vt_bytes * (m + 1)) > bstage_cap ||
+                    m + 1 > 4096))
+        break;
       m++;
       ne += k;
     }
     ch.nrows = m;
+    ch.nent = ne;
     ch.diag_off = (int)a16(16ll * m);
-    ch.ent_off = (int)(ch.diag_off + a16((long long)vt_bytes * m));
-    ch.img_bytes = (int)a16(ch.ent_off + (long long)ent_bytes * ne);
+    ch.val_off = (int)(ch.diag_off + a16((long long)vt_bytes * m));
+    ch.src_off = (int)(ch.val_off + a16((long long)vt_bytes * ne));
+    ch.img_bytes = (int)img_size(m, ne);
     ch.img_off = img_off;
     ch.b_off = b_off;
     ch.b_bytes = (int)a16((long long)vt_bytes * m);
     img_off += ch.img_bytes;
-    b_off += (int)(((m + b_align - 1) / b_align) * b_align);
-    for (int r = 0; r < m; r++) chunk_of[p + r] = (int)w.chunks.size();
+    b_off += ((m + b_align - 1) / b_align) * b_align;
+    for (int r = 0; r < m; r++) chunk_end[p + r] = p + m;
     w.chunks.push_back(ch);
     p += m;
   }
+  // sources outside the ring: pin the most-read ones in a fixed shared-memory table
+  std::vector<int> far_reads(n, 0);
+  for (int i = 0; i < n; i++)
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) {
+      const int j = dep[q];
+      if (chunk_end[pos[i]] - 1 - pos[j] >= ring) far_reads[j]++;
+    }
+  std::vector<int> cand;
+  for (int j = 0; j < n; j++)
+    if (far_reads[j]) cand.push_back(j);
+  std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return far_reads[a] > far_reads[b]; });
+  std::vector<int> pin_slot(n, -1);
+  for (size_t k = 0; k < cand.size() && (int)k < pin; k++) pin_slot[cand[k]] = (int)k;
+  w.pinned = (int)std::min<size_t>(cand.size(), (size_t)pin);
   w.img_bytes = img_off;
   w.blev_len = b_off + 16;
   w.order = order;
   w.bidx.resize(n);
   std::vector<unsigned char> img((size_t)img_off, 0);
-  for (size_t c = 0; c < w.chunks.size(); c++) {
-    const WaveChunk& ch = w.chunks[c];
+  for (const WaveChunk& ch : w.chunks) {
     int e = 0;
     for (int r = 0; r < ch.nrows; r++) {
       const int pp = ch.pos0 + r;
       const int i = order[pp];
       w.bidx[pp] = ch.b_off + r;
       const int k = ptr[i + 1] - ptr[i];
-      int4 mt = make_int4(i, e, k, 0);
-      std::memcpy(&img[(size_t)ch.img_off + 16 * (size_t)r], &mt, 16);
+      int mt[4] = {i, e, k, pin_slot[i] >= 0 ? ring + pin_slot[i] : -1};
+      std::memcpy(&img[(size_t)ch.img_off + 16 * (size_t)r], mt, 16);
       if (!lower) {
         w.diag_dst.push_back(ch.img_off + ch.diag_off + (long long)vt_bytes * r);
         w.diag_src.push_back(diag_pos[i]);
       }
-      // end position of this chunk: everything up to it has been written
-      const int chunk_end = ch.pos0 + ch.nrows;
+      const int cend = ch.pos0 + ch.nrows;
       for (int q = ptr[i]; q < ptr[i + 1]; q++, e++) {
         const int j = dep[q];
         const int pj = pos[j];
-        int src = (chunk_end - 1 - pj < ring) ? (pj % ring) : -(j + 1);
-        const long long off = ch.img_off + ch.ent_off + (long long)ent_bytes * e;
-        std::memcpy(&img[(size_t)off + vt_bytes], &src, 4);
-        w.ent_dst.push_back(off);
+        int src;
+        if (cend - 1 - pj < ring)
+          src = pj % ring;
+        else if (pin_slot[j] >= 0)
+          src = ring + pin_slot[j];
+        else
+          src = -(j + 1);
+        std::memcpy(&img[(size_t)(ch.img_off + ch.src_off) + 4 * (size_t)e], &src, 4);
+        w.ent_dst.push_back(ch.img_off + ch.val_off + (long long)vt_bytes * e);
         w.ent_src.push_back(src_pos[q]);
         if (src < 0) w.ring_misses++;
       }
@@ -109,4 +130,3 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   w.img_host.swap(img);
   return w;
 }
-

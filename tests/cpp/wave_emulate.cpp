@@ -27,7 +27,7 @@ static int fails = 0;
   } while (0)
 
 template <class VT>
-static void run(int n, int band, int seed, bool lower, int ring, int stage_cap, int bstage_cap) {
+static void run(int n, int band, int seed, bool lower, int ring, int pin, int stage_cap, int bstage_cap) {
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> U(-1.0, 1.0);
   // random triangular structure within a band
@@ -54,7 +54,7 @@ static void run(int n, int band, int seed, bool lower, int ring, int stage_cap, 
     val.push_back(1.5 + U(rng) * 0.2);
   }
   const int vtb = sizeof(VT);
-  WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, stage_cap, bstage_cap);
+  WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, pin, stage_cap, bstage_cap);
   // pack values as the device kernel does
   std::vector<unsigned char> img = w.img_host;
   for (size_t q = 0; q < w.ent_dst.size(); q++) {
@@ -77,12 +77,12 @@ static void run(int n, int band, int seed, bool lower, int ring, int stage_cap, 
     for (int q = ptr[i]; q < ptr[i + 1]; q++) acc += (VT)val[srcpos[q]] * xr[dep[q]];
     xr[i] = lower ? b[i] + acc : (b[i] - acc) / (VT)val[diag_pos[i]];
   }
-  const int entb = (vtb == 8) ? 16 : 8;
   for (int pass = 0; pass < 2; pass++) {
-    std::vector<VT> ringv(ring, (VT)NAN), x(n, (VT)NAN);
+    std::vector<VT> ringv(ring + pin, (VT)NAN), x(n, (VT)NAN);
     int written = 0;
     for (const WaveChunk& ch : w.chunks) {
       CHECK(ch.img_off % 16 == 0 && ch.img_bytes % 16 == 0, "image alignment");
+      CHECK(ch.diag_off % 16 == 0 && ch.val_off % 16 == 0 && ch.src_off % 16 == 0, "part alignment");
       CHECK(ch.img_bytes <= stage_cap || ch.nrows == 1, "stage capacity %d > %d", ch.img_bytes, stage_cap);
       CHECK((ch.b_off * vtb) % 16 == 0 && ch.b_bytes % 16 == 0, "rhs alignment");
       CHECK(ch.b_bytes <= bstage_cap, "rhs stage capacity");
@@ -96,8 +96,9 @@ static void run(int n, int band, int seed, bool lower, int ring, int stage_cap, 
         for (int e = meta[1]; e < meta[1] + meta[2]; e++) {
           VT v;
           int src;
-          std::memcpy(&v, st + ch.ent_off + (size_t)entb * e, sizeof(VT));
-          std::memcpy(&src, st + ch.ent_off + (size_t)entb * e + vtb, 4);
+          std::memcpy(&v, st + ch.val_off + (size_t)vtb * e, sizeof(VT));
+          std::memcpy(&src, st + ch.src_off + (size_t)4 * e, 4);
+          CHECK(src < ring + pin, "source slot out of range");
           VT xv = src >= 0 ? ringv[src] : x[-src - 1];
           acc += v * xv;
         }
@@ -111,6 +112,10 @@ static void run(int n, int band, int seed, bool lower, int ring, int stage_cap, 
           xi = (bv - acc) / d;
         }
         ringv[(ch.pos0 + r) % ring] = xi;
+        if (meta[3] >= 0) {
+          CHECK(meta[3] >= ring && meta[3] < ring + pin, "pinned slot out of range");
+          ringv[meta[3]] = xi;
+        }
         x[meta[0]] = xi;
       }
       written += ch.nrows;
@@ -131,11 +136,12 @@ int main() {
   for (int lower = 0; lower < 2; lower++) {
     for (int n : {1, 2, 7, 64, 1000, 20000}) {
       for (int band : {1, 3, 50, 600}) {
-        run<double>(n, band, n + band, lower, 8192, 40960, 4096);
-        run<float>(n, band, n + band + 1, lower, 16384, 40960, 4096);
-        // tiny ring and stages force ring misses and level splitting
-        run<double>(n, band, n + band + 2, lower, 64, 1024, 64);
-        run<float>(n, band, n + band + 3, lower, 32, 512, 32);
+        run<double>(n, band, n + band, lower, kWaveRing, kWavePin, kWaveStage64, kWaveBStage64);
+        run<float>(n, band, n + band + 1, lower, kWaveRing, kWavePin, kWaveStage32, kWaveBStage32);
+        // tiny rings, pinned tables and stages force pinning, global reads and level splitting
+        run<double>(n, band, n + band + 2, lower, 64, 16, 1024, 64);
+        run<float>(n, band, n + band + 3, lower, 32, 0, 512, 32);
+        run<float>(n, band, n + band + 4, lower, 16, 4096, 512, 32);
       }
     }
   }
