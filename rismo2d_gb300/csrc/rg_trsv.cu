@@ -26,7 +26,7 @@ namespace {
 
 constexpr int kThreads = 1024;
 constexpr int kGroup = 4;                 // threads per row
-constexpr long long kMbarSpin = 1ll << 24;
+constexpr long long kMbarSpin = 1ll << 26;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -68,6 +68,27 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 namespace {
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// bounded wait on an mbarrier phase; false when the bound ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  long long it = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++it > kMbarSpin) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void consumers_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");
+}
+
+// Warp-specialised wavefront solve: warp 31 (one elected lane) is the producer
+// that streams chunk images and right-hand sides into NST stages with
+// cp.async.bulk; warps 0..30 consume the stages in order, one dependency level
+// chunk at a time, synchronising on a named barrier between chunks.
 template <class VT, bool LOWER, int RING, int PIN>
 __global__ void __launch_bounds__(kThreads, 1)
     k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, const unsigned char* __restrict__ img,
@@ -76,41 +97,53 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (ks && ks->conv != 0) return;
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int NST = 3;
+  constexpr int kConsumers = kThreads - 32;
   // solution values: ring slots [0, RING), pinned long-range slots [RING, RING + PIN)
   VT* vals = reinterpret_cast<VT*>(smem);
   unsigned char* stage0 = smem + (RING + PIN) * sizeof(VT);
   unsigned char* bstage0 = stage0 + NST * (size_t)stage_bytes;
-  __shared__ __align__(8) uint64_t bars[NST];
-  __shared__ int abort_flag;
+  __shared__ __align__(8) uint64_t full[NST];
+  __shared__ __align__(8) uint64_t empty[NST];
+  __shared__ WaveChunk sdesc[NST];
   const int tid = threadIdx.x;
   if (tid == 0) {
-    abort_flag = 0;
-    for (int s = 0; s < NST; s++) mbar_init(&bars[s], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    for (int s = 0; s < NST && s < nchunks; s++) {
-      const WaveChunk ch = chunks[s];
-      mbar_expect_tx(&bars[s], (unsigned)(ch.img_bytes + ch.b_bytes));
-      bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &bars[s]);
-      bulk_g2s(bstage0 + s * (size_t)bstage_bytes, blev + ch.b_off, (unsigned)ch.b_bytes, &bars[s]);
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
     }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
-  const int g = tid & (kGroup - 1);
-  const int rows_per_pass = kThreads / kGroup;
-  for (int k = 0; k < nchunks; k++) {
-    const int s = k % NST;
-    const unsigned parity = (unsigned)((k / NST) & 1);
-    {
-      long long it = 0;
-      while (!mbar_try_wait(&bars[s], parity)) {
-        if (++it > kMbarSpin) {
-          if (atomicExch(&abort_flag, 1) == 0) atomicOr(err, 8);
+  if (tid >= kConsumers) {
+    // ---- producer ------------------------------------------------------------
+    if (tid == kConsumers) {
+      for (int k = 0; k < nchunks; k++) {
+        const int s = k % NST;
+        if (k >= NST && !mbar_wait_bounded(&empty[s], (unsigned)(((k / NST) - 1) & 1))) {
+          atomicOr(err, 8);
           break;
         }
+        const WaveChunk ch = chunks[k];
+        sdesc[s] = ch;
+        fence_proxy_async();   // earlier generic reads of the stage precede the async refill
+        mbar_expect_tx(&full[s], (unsigned)(ch.img_bytes + ch.b_bytes));
+        bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s]);
+        bulk_g2s(bstage0 + s * (size_t)bstage_bytes, blev + ch.b_off, (unsigned)ch.b_bytes, &full[s]);
       }
     }
-    const WaveChunk ch = chunks[k];
+    return;
+  }
+
+  // ---- consumers -------------------------------------------------------------
+  const int g = tid & (kGroup - 1);
+  const int rows_per_pass = kConsumers / kGroup;
+  for (int k = 0; k < nchunks; k++) {
+    const int s = k % NST;
+    if (!mbar_wait_bounded(&full[s], (unsigned)((k / NST) & 1))) {
+      if (tid == 0) atomicOr(err, 8);
+    }
+    const WaveChunk ch = sdesc[s];
     const unsigned char* st = stage0 + s * (size_t)stage_bytes;
     const int4* meta = reinterpret_cast<const int4*>(st);
     const VT* diag = reinterpret_cast<const VT*>(st + ch.diag_off);
@@ -144,14 +177,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         x[mt.x] = xi;
       }
     }
-    __syncthreads();
-    if (tid == 0 && k + NST < nchunks) {
-      const WaveChunk nx = chunks[k + NST];
-      fence_proxy_async();   // generic reads of this stage happen before the async refill
-      mbar_expect_tx(&bars[s], (unsigned)(nx.img_bytes + nx.b_bytes));
-      bulk_g2s(stage0 + s * (size_t)stage_bytes, img + nx.img_off, (unsigned)nx.img_bytes, &bars[s]);
-      bulk_g2s(bstage0 + s * (size_t)bstage_bytes, blev + nx.b_off, (unsigned)nx.b_bytes, &bars[s]);
-    }
+    consumers_sync();                 // chunk k complete: its values are visible, its stage is free
+    if (tid == 0) mbar_arrive(&empty[s]);
   }
 }
 
