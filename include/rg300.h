@@ -174,8 +174,20 @@ rg_status rg_get_timings(rg_ctx* ctx, double* ms, int n);
 /* Structure of the resident system: [0] neq, [1] nnz, [2] dependency depth of
  * the L solve, [3] of the U solve, [4] element colours, [5] L entries,
  * [6] / [7] wavefront chunks of the L / U solve, [8] / [9] their entries whose
- * source lies outside the shared-memory ring. */
+ * source lies outside the shared-memory ring, [10] factorisations redone by
+ * the zero-pivot repair path, [11] factorisations, [12] / [13] bytes copied
+ * host->device / device->host by this context's calls so far, [14] kernels
+ * launched so far. */
 rg_status rg_get_stats(rg_ctx* ctx, int64_t* out, int n);
+
+/* Per-kernel device time, for measurement.  While enabled, every launch of the
+ * triangular solves (class 0), SpMV (1), ILU(0) factorisation (2) and element
+ * assembly (3) is bracketed by CUDA events on the context's stream; the
+ * elapsed times are summed when a call synchronises.  rg_profile_read gives
+ * out[2k] = launches and out[2k+1] = total milliseconds of class k.  No
+ * counterpart in the reference, which times with the host clock only. */
+rg_status rg_profile(rg_ctx* ctx, int enable, int reset);
+rg_status rg_profile_read(rg_ctx* ctx, double* out, int n);
 
 /* CUDA events on the context's stream (8 slots), for timing a caller's
  * sequence of calls on the device clock. */

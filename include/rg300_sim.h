@@ -122,6 +122,13 @@ rg_status rg_sim_dry_rewet(rg_sim* sim, int* dried, int* wetted);
 rg_status rg_sim_get_numbering(rg_sim* sim, int* neq, int* eqno, int* width, int64_t* nnz);
 rg_status rg_sim_get_pattern(rg_sim* sim, int* index);
 rg_status rg_sim_get_boundary(rg_sim* sim, int* nflag, int* bckind, double* rot4, double* bcU, double* bcS);
+/* the model element list of the last model build (MODEL::Initialize
+ * Model.cpp:121-216): *ne elements, 6 node slots each (boundary lines use the
+ * first three: corner, corner, mid-side), node count (6 or 3), ELEM::flag and
+ * eddy viscosity; plus the open-boundary normal per node (NODE::niox/nioy).
+ * NULL skips an output; call with only `ne` first to size the arrays. */
+rg_status rg_sim_get_model(rg_sim* sim, int* ne, int* elem_nodes, int* elem_nnd, int* elem_flag, double* elem_vt,
+                           double* niox, double* nioy);
 
 /* the GPU context of a simulation (for rg_get_stats, rg_event_*, timings) */
 rg_ctx* rg_sim_context(rg_sim* sim);

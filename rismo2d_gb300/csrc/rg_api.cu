@@ -29,11 +29,26 @@ rg_status rg_cuda(rg_ctx* c, cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return rg_cuda(c, _e, #expr); \
   } while (0)
 
+// host <-> device copies on the context's stream, counted for rg_get_stats
+static cudaError_t rg_copy(rg_ctx* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+  if (kind == cudaMemcpyHostToDevice) c->h2d_bytes += (long long)bytes;
+  if (kind == cudaMemcpyDeviceToHost) c->d2h_bytes += (long long)bytes;
+  return cudaMemcpyAsync(dst, src, bytes, kind, c->st);
+}
+
+static cudaError_t h2d(rg_ctx* c, void* d, const void* h, size_t bytes) {
+  return rg_copy(c, d, h, bytes, cudaMemcpyHostToDevice);
+}
+
+static cudaError_t d2h(rg_ctx* c, void* h, const void* d, size_t bytes) {
+  return rg_copy(c, h, d, bytes, cudaMemcpyDeviceToHost);
+}
+
 template <class T>
 static cudaError_t upload(rg_ctx* c, DBuf<T>& d, const T* h, size_t n) {
   cudaError_t e = d.alloc(n);
   if (e != cudaSuccess || n == 0 || !h) return e;
-  return cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->st);
+  return h2d(c, d.p, h, n * sizeof(T));
 }
 
 template <class T>
@@ -43,11 +58,45 @@ static cudaError_t upload_if(rg_ctx* c, DBuf<T>& d, const T* h, size_t n) {
     cudaError_t e = d.alloc(n);
     if (e != cudaSuccess) return e;
   }
-  return cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->st);
+  return h2d(c, d.p, h, n * sizeof(T));
+}
+
+// ---- per-kernel-class event accounting ---------------------------------------
+
+cudaError_t prof_flush(rg_ctx* c) {
+  if (c->prof_used == 0) return cudaSuccess;
+  cudaError_t e = cudaEventSynchronize(c->prof_ev[2 * (c->prof_used - 1) + 1]);
+  if (e != cudaSuccess) return e;
+  for (int i = 0; i < c->prof_used; i++) {
+    float ms = 0;
+    e = cudaEventElapsedTime(&ms, c->prof_ev[2 * i], c->prof_ev[2 * i + 1]);
+    if (e != cudaSuccess) return e;
+    c->prof_ms[c->prof_cls[i]] += ms;
+    c->prof_launches[c->prof_cls[i]]++;
+  }
+  c->prof_used = 0;
+  return cudaSuccess;
+}
+
+cudaError_t prof_begin(rg_ctx* c, int cls) {
+  if (!c->prof_on) return cudaSuccess;
+  if (c->prof_used == rg_ctx::kProfPairs) {
+    cudaError_t e = prof_flush(c);
+    if (e != cudaSuccess) return e;
+  }
+  c->prof_cls[c->prof_used] = cls;
+  return cudaEventRecord(c->prof_ev[2 * c->prof_used], c->st);
+}
+
+cudaError_t prof_end(rg_ctx* c) {
+  if (!c->prof_on) return cudaSuccess;
+  cudaError_t e = cudaEventRecord(c->prof_ev[2 * c->prof_used + 1], c->st);
+  c->prof_used++;
+  return e;
 }
 
 static rg_status check_device_error(rg_ctx* c) {
-  TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  TRY(d2h(c, c->err_host, c->dev_err.p, 4 * sizeof(int)));
   TRY(cudaStreamSynchronize(c->st));
   int e = c->err_host[0];
   if (e == 0) return RG_OK;
@@ -210,16 +259,16 @@ cudaError_t launch_update(rg_ctx* c, const rg_update_opts* o, double* stats) {
   int nb = (c->np_model + 255) / 256;
   if (nb > c->num_sms * 8) nb = c->num_sms * 8;
   if (nb < 1) nb = 1;
-  k_upd_reduce<<<nb, 256, 0, c->st>>>(c->np_model, c->model_nodes.p, c->eqno.p, c->X.p, c->upd.p);
-  k_upd_relax<<<1, 1, 0, c->st>>>(c->upd.p, o->relax_method, o->max_delta_uv, o->max_delta_s);
-  k_upd_apply<<<nb, 256, 0, c->st>>>(c->np_model, c->model_nodes.p, c->eqno.p, c->nflag.p, c->rot.p, c->X.p,
+  k_upd_reduce<<<nb, 256, 0, rg_counted(c)>>>(c->np_model, c->model_nodes.p, c->eqno.p, c->X.p, c->upd.p);
+  k_upd_relax<<<1, 1, 0, rg_counted(c)>>>(c->upd.p, o->relax_method, o->max_delta_uv, o->max_delta_s);
+  k_upd_apply<<<nb, 256, 0, rg_counted(c)>>>(c->np_model, c->model_nodes.p, c->eqno.p, c->nflag.p, c->rot.p, c->X.p,
                                      c->upd.p, c->U.p, c->V.p, c->S.p, c->z.p, c->zor.p, o->max_us, o->dry_limit,
                                      o->dryrew_method, c->hmin);
   int nbe = (c->ne_region + 255) / 256;
   if (nbe < 1) nbe = 1;
-  k_upd_midside<<<nbe, 256, 0, c->st>>>(c->ne_region, c->region_nodes.p, c->S.p, c->z.p);
+  k_upd_midside<<<nbe, 256, 0, rg_counted(c)>>>(c->ne_region, c->region_nodes.p, c->S.p, c->z.p);
   double h[16];
-  e = cudaMemcpyAsync(h, c->upd.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+  e = rg_copy(c, h, c->upd.p, 16 * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return e;
   e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return e;
@@ -318,6 +367,7 @@ rg_status rg_destroy(rg_ctx* c) {
   if (c->err_host) cudaFreeHost(c->err_host);
   for (int i = 0; i < 16; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return RG_OK;
@@ -593,10 +643,10 @@ rg_status rg_get_state(rg_ctx* c, double* U, double* V, double* S, double* z) {
   if (!c) return RG_ERR_ARG;
   TRY(cudaSetDevice(c->device));
   const size_t b = c->np * sizeof(double);
-  if (U) TRY(cudaMemcpyAsync(U, c->U.p, b, cudaMemcpyDeviceToHost, c->st));
-  if (V) TRY(cudaMemcpyAsync(V, c->V.p, b, cudaMemcpyDeviceToHost, c->st));
-  if (S) TRY(cudaMemcpyAsync(S, c->S.p, b, cudaMemcpyDeviceToHost, c->st));
-  if (z) TRY(cudaMemcpyAsync(z, c->z.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (U) TRY(rg_copy(c, U, c->U.p, b, cudaMemcpyDeviceToHost));
+  if (V) TRY(rg_copy(c, V, c->V.p, b, cudaMemcpyDeviceToHost));
+  if (S) TRY(rg_copy(c, S, c->S.p, b, cudaMemcpyDeviceToHost));
+  if (z) TRY(rg_copy(c, z, c->z.p, b, cudaMemcpyDeviceToHost));
   TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
 }
@@ -609,22 +659,22 @@ rg_status rg_set_relax(rg_ctx* c, double relaxThdt_UV, double relaxThdt_H) {
 }
 
 static rg_status copy_out_system(rg_ctx* c, double* B_out, float* A32_out, double* A64_out, bool lu) {
-  if (B_out) TRY(cudaMemcpyAsync(B_out, c->B.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (B_out) TRY(rg_copy(c, B_out, c->B.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost));
   if (c->prec == RG_PREC_FP64) {
     const double* src = lu ? c->LU64.p : c->A64.p;
-    if (A64_out) TRY(cudaMemcpyAsync(A64_out, src, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    if (A64_out) TRY(rg_copy(c, A64_out, src, c->nnz * sizeof(double), cudaMemcpyDeviceToHost));
     if (A32_out) {
       std::vector<double> tmp(c->nnz);
-      TRY(cudaMemcpyAsync(tmp.data(), src, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      TRY(rg_copy(c, tmp.data(), src, c->nnz * sizeof(double), cudaMemcpyDeviceToHost));
       TRY(cudaStreamSynchronize(c->st));
       for (int64_t i = 0; i < c->nnz; i++) A32_out[i] = (float)tmp[i];
     }
   } else {
     const float* src = lu ? c->LU32.p : c->A32.p;
-    if (A32_out) TRY(cudaMemcpyAsync(A32_out, src, c->nnz * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    if (A32_out) TRY(rg_copy(c, A32_out, src, c->nnz * sizeof(float), cudaMemcpyDeviceToHost));
     if (A64_out) {
       std::vector<float> tmp(c->nnz);
-      TRY(cudaMemcpyAsync(tmp.data(), src, c->nnz * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+      TRY(rg_copy(c, tmp.data(), src, c->nnz * sizeof(float), cudaMemcpyDeviceToHost));
       TRY(cudaStreamSynchronize(c->st));
       for (int64_t i = 0; i < c->nnz; i++) A64_out[i] = (double)tmp[i];
     }
@@ -637,7 +687,9 @@ rg_status rg_assemble(rg_ctx* c, double* B_out, float* A32_out, double* A64_out)
   if (!c || c->neq <= 0) return rg_fail(c, RG_ERR_ARG, "rg_assemble: no pattern");
   TRY(cudaSetDevice(c->device));
   TRY(cudaEventRecord(c->ev[0], c->st));
+  TRY(prof_begin(c, RG_PROF_ASSEMBLE));
   TRY(launch_assemble(c));
+  TRY(prof_end(c));
   TRY(cudaEventRecord(c->ev[1], c->st));
   TRY(cudaEventSynchronize(c->ev[1]));
   float ms = 0;
@@ -653,23 +705,23 @@ rg_status rg_load_system(rg_ctx* c, const float* A32, const double* A64, const d
   TRY(cudaSetDevice(c->device));
   if (c->prec == RG_PREC_FP64) {
     if (A64) {
-      TRY(cudaMemcpyAsync(c->A64.p, A64, c->nnz * sizeof(double), cudaMemcpyHostToDevice, c->st));
+      TRY(rg_copy(c, c->A64.p, A64, c->nnz * sizeof(double), cudaMemcpyHostToDevice));
     } else {
       std::vector<double> t(A32, A32 + c->nnz);
-      TRY(cudaMemcpyAsync(c->A64.p, t.data(), c->nnz * sizeof(double), cudaMemcpyHostToDevice, c->st));
+      TRY(rg_copy(c, c->A64.p, t.data(), c->nnz * sizeof(double), cudaMemcpyHostToDevice));
       TRY(cudaStreamSynchronize(c->st));
     }
   } else {
     if (A32) {
-      TRY(cudaMemcpyAsync(c->A32.p, A32, c->nnz * sizeof(float), cudaMemcpyHostToDevice, c->st));
+      TRY(rg_copy(c, c->A32.p, A32, c->nnz * sizeof(float), cudaMemcpyHostToDevice));
     } else {
       std::vector<float> t(c->nnz);
       for (int64_t i = 0; i < c->nnz; i++) t[i] = (float)A64[i];
-      TRY(cudaMemcpyAsync(c->A32.p, t.data(), c->nnz * sizeof(float), cudaMemcpyHostToDevice, c->st));
+      TRY(rg_copy(c, c->A32.p, t.data(), c->nnz * sizeof(float), cudaMemcpyHostToDevice));
       TRY(cudaStreamSynchronize(c->st));
     }
   }
-  TRY(cudaMemcpyAsync(c->B.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  TRY(rg_copy(c, c->B.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice));
   TRY(cudaStreamSynchronize(c->st));
   c->have_system = true;
   c->have_factor = false;
@@ -698,9 +750,11 @@ rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
   TRY(cudaEventRecord(c->ev[4], c->st));
   c->n_factor_calls++;
   if (c->use_level_factor) {
+    TRY(prof_begin(c, RG_PROF_FACTOR));
     TRY(launch_factor_level(c));
+    TRY(prof_end(c));
     TRY(cudaEventRecord(c->ev[6], c->st));
-    TRY(cudaMemcpyAsync(c->err_host, c->dev_err.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    TRY(d2h(c, c->err_host, c->dev_err.p, 4 * sizeof(int)));
     TRY(cudaStreamSynchronize(c->st));
     if (c->err_host[0] & 16) {
       // a pivot needs the zero-pivot repair: redo with the dependency-driven kernel
@@ -731,7 +785,7 @@ rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
 rg_status rg_ilu0_apply(rg_ctx* c, const double* B, double* X) {
   if (!c || !c->have_factor || !B || !X) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply: no factors");
   TRY(cudaSetDevice(c->device));
-  TRY(cudaMemcpyAsync(c->ri.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  TRY(rg_copy(c, c->ri.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice));
   TRY(cudaEventRecord(c->ev[6], c->st));
   TRY(launch_ilu_apply_d(c, c->ri.p, c->zi.p));
   TRY(cudaEventRecord(c->ev[7], c->st));
@@ -740,7 +794,7 @@ rg_status rg_ilu0_apply(rg_ctx* c, const double* B, double* X) {
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
   c->t_ms[5] = ms;
-  TRY(cudaMemcpyAsync(X, c->zi.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(rg_copy(c, X, c->zi.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost));
   TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
 }
@@ -748,11 +802,11 @@ rg_status rg_ilu0_apply(rg_ctx* c, const double* B, double* X) {
 rg_status rg_spmv(rg_ctx* c, const double* x, double* r) {
   if (!c || !c->have_system || !x || !r) return rg_fail(c, RG_ERR_ARG, "rg_spmv: no system");
   TRY(cudaSetDevice(c->device));
-  TRY(cudaMemcpyAsync(c->pi.p, x, c->neq * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  TRY(rg_copy(c, c->pi.p, x, c->neq * sizeof(double), cudaMemcpyHostToDevice));
   TRY(cudaEventRecord(c->ev[8], c->st));
   TRY(launch_spmv_d(c, c->pi.p, c->vi.p));
   TRY(cudaEventRecord(c->ev[9], c->st));
-  TRY(cudaMemcpyAsync(r, c->vi.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(rg_copy(c, r, c->vi.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost));
   TRY(cudaStreamSynchronize(c->st));
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[8], c->ev[9]));
@@ -772,8 +826,9 @@ rg_status rg_bicgstab(rg_ctx* c, int maxIter, double maxDiff, double* X_out, int
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[10], c->ev[11]));
   c->t_ms[3] = ms;
+  TRY(prof_flush(c));
   if (X_out) {
-    TRY(cudaMemcpyAsync(X_out, c->X.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    TRY(rg_copy(c, X_out, c->X.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost));
     TRY(cudaStreamSynchronize(c->st));
   }
   return s;
@@ -856,7 +911,7 @@ rg_status rg_friction(rg_ctx* c, double* cf_out) {
   TRY(cudaEventRecord(c->ev[14], c->st));
   TRY(launch_friction(c));
   TRY(cudaEventRecord(c->ev[15], c->st));
-  if (cf_out) TRY(cudaMemcpyAsync(cf_out, c->cf.p, c->np * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (cf_out) TRY(rg_copy(c, cf_out, c->cf.p, c->np * sizeof(double), cudaMemcpyDeviceToHost));
   TRY(cudaStreamSynchronize(c->st));
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[14], c->ev[15]));
@@ -907,9 +962,9 @@ rg_status rg_get_dt(rg_ctx* c, double* dUdt, double* dVdt, double* dSdt) {
   if (!c) return RG_ERR_ARG;
   TRY(cudaSetDevice(c->device));
   const size_t b = c->np * sizeof(double);
-  if (dUdt) TRY(cudaMemcpyAsync(dUdt, c->dUdt.p, b, cudaMemcpyDeviceToHost, c->st));
-  if (dVdt) TRY(cudaMemcpyAsync(dVdt, c->dVdt.p, b, cudaMemcpyDeviceToHost, c->st));
-  if (dSdt) TRY(cudaMemcpyAsync(dSdt, c->dSdt.p, b, cudaMemcpyDeviceToHost, c->st));
+  if (dUdt) TRY(rg_copy(c, dUdt, c->dUdt.p, b, cudaMemcpyDeviceToHost));
+  if (dVdt) TRY(rg_copy(c, dVdt, c->dVdt.p, b, cudaMemcpyDeviceToHost));
+  if (dSdt) TRY(rg_copy(c, dSdt, c->dSdt.p, b, cudaMemcpyDeviceToHost));
   TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
 }
@@ -921,7 +976,7 @@ rg_status rg_timegrad(rg_ctx* c, double dt, double theta) {
   const double iTheta = 1.0 - 1.0 / theta, thdt = 1.0 / dt / theta;
   int nb = (c->np + 255) / 256;
   if (nb > c->num_sms * 8) nb = c->num_sms * 8;
-  k_timegrad<<<nb, 256, 0, c->st>>>(c->np, c->nflag.p, c->U.p, c->V.p, c->S.p, c->oU.p, c->oV.p, c->oS.p,
+  k_timegrad<<<nb, 256, 0, rg_counted(c)>>>(c->np, c->nflag.p, c->U.p, c->V.p, c->S.p, c->oU.p, c->oV.p, c->oS.p,
                                     c->odUdt.p, c->odVdt.p, c->odSdt.p, c->dUdt.p, c->dVdt.p, c->dSdt.p, iTheta,
                                     thdt);
   TRY(cudaGetLastError());
@@ -935,17 +990,47 @@ rg_status rg_zero_velocity(rg_ctx* c, int n, const int* nodes) {
     if (nodes[i] < 0 || nodes[i] >= c->np) return rg_fail(c, RG_ERR_ARG, "rg_zero_velocity: node out of range");
   TRY(cudaSetDevice(c->device));
   TRY(upload(c, c->zero_nodes, nodes, n));
-  k_zero_uv<<<(n + 255) / 256, 256, 0, c->st>>>(n, c->zero_nodes.p, c->U.p, c->V.p);
+  k_zero_uv<<<(n + 255) / 256, 256, 0, rg_counted(c)>>>(n, c->zero_nodes.p, c->U.p, c->V.p);
   TRY(cudaGetLastError());
   return RG_OK;
 }
 
 rg_status rg_get_stats(rg_ctx* c, int64_t* out, int n) {
   if (!c || !out) return RG_ERR_ARG;
-  int64_t v[12] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n,
+  int64_t v[15] = {c->neq, c->nnz, c->depth_L, c->depth_U, c->n_colors, (int64_t)c->Lcol.n,
                     c->waveL.nchunks, c->waveU.nchunks, c->waveL.ring_misses, c->waveU.ring_misses,
-                    c->n_repair_fallbacks, c->n_factor_calls};
-  for (int i = 0; i < n && i < 12; i++) out[i] = v[i];
+                    c->n_repair_fallbacks, c->n_factor_calls, c->h2d_bytes, c->d2h_bytes, c->n_launches};
+  for (int i = 0; i < n && i < 15; i++) out[i] = v[i];
+  return RG_OK;
+}
+
+rg_status rg_profile(rg_ctx* c, int enable, int reset) {
+  if (!c) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  if (c->prof_ev.empty() && enable) {
+    c->prof_ev.resize(2 * rg_ctx::kProfPairs, nullptr);
+    c->prof_cls.resize(rg_ctx::kProfPairs, 0);
+    for (cudaEvent_t& e : c->prof_ev) TRY(cudaEventCreate(&e));
+  }
+  TRY(prof_flush(c));
+  if (reset) {
+    for (int k = 0; k < rg_ctx::kProfClasses; k++) {
+      c->prof_launches[k] = 0;
+      c->prof_ms[k] = 0.0;
+    }
+  }
+  c->prof_on = enable != 0;
+  return RG_OK;
+}
+
+rg_status rg_profile_read(rg_ctx* c, double* out, int n) {
+  if (!c || !out) return RG_ERR_ARG;
+  TRY(cudaSetDevice(c->device));
+  TRY(prof_flush(c));
+  for (int k = 0; k < rg_ctx::kProfClasses && 2 * k + 1 < n; k++) {
+    out[2 * k] = (double)c->prof_launches[k];
+    out[2 * k + 1] = c->prof_ms[k];
+  }
   return RG_OK;
 }
 

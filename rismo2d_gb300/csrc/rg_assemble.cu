@@ -616,10 +616,10 @@ cudaError_t launch_assemble(rg_ctx* c) {
   // zero A and B (CRSMAT::Init, CRSMat.cpp:206-212; Assemble.cpp:213)
   int zb = c->num_sms * 8;
   if (dbl)
-    k_zero<double><<<zb, 256, 0, c->st>>>(c->A64.p, c->nnz);
+    k_zero<double><<<zb, 256, 0, rg_counted(c)>>>(c->A64.p, c->nnz);
   else
-    k_zero<float><<<zb, 256, 0, c->st>>>(c->A32.p, c->nnz);
-  k_zero<double><<<zb, 256, 0, c->st>>>(c->B.p, c->neq);
+    k_zero<float><<<zb, 256, 0, rg_counted(c)>>>(c->A32.p, c->nnz);
+  k_zero<double><<<zb, 256, 0, rg_counted(c)>>>(c->B.p, c->neq);
 
   AsmArgs a;
   a.x = c->x.p; a.y = c->y.p; a.z = c->z.p; a.U = c->U.p; a.V = c->V.p; a.S = c->S.p;
@@ -639,15 +639,15 @@ cudaError_t launch_assemble(rg_ctx* c) {
       if (c->prec == RG_PREC_FP64) {
         int blocks = (a.count + 1) / 2;
         if (blocks > c->num_sms * 32) blocks = c->num_sms * 32;
-        k_region<double, double, 2><<<blocks, 64, 0, c->st>>>(a, c->A64.p);
+        k_region<double, double, 2><<<blocks, 64, 0, rg_counted(c)>>>(a, c->A64.p);
       } else if (c->prec == RG_PREC_REF32) {
         int blocks = (a.count + 1) / 2;
         if (blocks > c->num_sms * 32) blocks = c->num_sms * 32;
-        k_region<double, float, 2><<<blocks, 64, 0, c->st>>>(a, c->A32.p);
+        k_region<double, float, 2><<<blocks, 64, 0, rg_counted(c)>>>(a, c->A32.p);
       } else {
         int blocks = (a.count + 3) / 4;
         if (blocks > c->num_sms * 16) blocks = c->num_sms * 16;
-        k_region<float, float, 4><<<blocks, 128, 0, c->st>>>(a, c->A32.p);
+        k_region<float, float, 4><<<blocks, 128, 0, rg_counted(c)>>>(a, c->A32.p);
       }
     }
     if (be > re) {
@@ -655,9 +655,9 @@ cudaError_t launch_assemble(rg_ctx* c) {
       a.count = be - re;
       int blocks = (a.count + 63) / 64;
       if (dbl)
-        k_bound<double><<<blocks, 64, 0, c->st>>>(a, c->A64.p);
+        k_bound<double><<<blocks, 64, 0, rg_counted(c)>>>(a, c->A64.p);
       else
-        k_bound<float><<<blocks, 64, 0, c->st>>>(a, c->A32.p);
+        k_bound<float><<<blocks, 64, 0, rg_counted(c)>>>(a, c->A32.p);
     }
   }
   return cudaGetLastError();
@@ -665,7 +665,7 @@ cudaError_t launch_assemble(rg_ctx* c) {
 
 cudaError_t launch_friction(rg_ctx* c) {
   int np = c->np;
-  k_friction<<<(np + 255) / 256, 256, 0, c->st>>>(np, c->fr_ptr.p, c->fr_el.p, c->elem_n.p, c->elem_af.p,
+  k_friction<<<(np + 255) / 256, 256, 0, rg_counted(c)>>>(np, c->fr_ptr.p, c->fr_el.p, c->elem_n.p, c->elem_af.p,
                                                    c->S.p, c->z.p, c->hmin, c->g, c->cf.p);
   return cudaGetLastError();
 }

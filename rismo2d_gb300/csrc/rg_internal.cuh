@@ -193,7 +193,36 @@ struct rg_ctx {
   int trace = 0;                // RG_TRACE level (diagnostics to stderr)   // dependency depth of the triangular solves
   cudaEvent_t user_ev[8];
   bool user_ev_ready = false;
+
+  // host <-> device bytes moved by the ABI calls, kernel launches (cumulative)
+  long long h2d_bytes = 0, d2h_bytes = 0;
+  long long n_launches = 0;
+
+  // per-kernel-class device time (rg_profile): event pairs around launches,
+  // summed whenever the pool fills or a call synchronises
+  static constexpr int kProfClasses = 4;
+  static constexpr int kProfPairs = 2048;
+  bool prof_on = false;
+  std::vector<cudaEvent_t> prof_ev;        // 2 * kProfPairs
+  std::vector<int> prof_cls;               // class of each recorded pair
+  int prof_used = 0;
+  long long prof_launches[kProfClasses] = {0};
+  double prof_ms[kProfClasses] = {0};
 };
+
+// the context's stream as a launch argument, counting the launch
+inline cudaStream_t rg_counted(rg_ctx* c) {
+  c->n_launches++;
+  return c->st;
+}
+
+// kernel classes of rg_profile
+enum { RG_PROF_TRSV = 0, RG_PROF_SPMV = 1, RG_PROF_FACTOR = 2, RG_PROF_ASSEMBLE = 3 };
+// open / close one timed launch of class `cls` (no-ops unless profiling)
+cudaError_t prof_begin(rg_ctx* c, int cls);
+cudaError_t prof_end(rg_ctx* c);
+// wait for the recorded pairs and add them to the sums
+cudaError_t prof_flush(rg_ctx* c);
 
 // ---- launchers implemented in the .cu files -------------------------------
 rg_status rg_fail(rg_ctx* c, rg_status s, const char* msg);

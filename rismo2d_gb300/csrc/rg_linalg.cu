@@ -779,12 +779,13 @@ static int grid_for(rg_ctx* c, int64_t n, int block) {
 
 cudaError_t launch_scale(rg_ctx* c, double* scale_host) {
   const int nb = grid_for(c, c->neq, 256);
-  k_sumsq<double><<<nb, 256, 0, c->st>>>(c->B.p, c->neq, c->partial.p);
-  k_scale_fin<<<1, 256, 0, c->st>>>(c->partial.p, nb, c->ks.p);
+  k_sumsq<double><<<nb, 256, 0, rg_counted(c)>>>(c->B.p, c->neq, c->partial.p);
+  k_scale_fin<<<1, 256, 0, rg_counted(c)>>>(c->partial.p, nb, c->ks.p);
   if (c->prec == RG_PREC_FP64)
-    k_scale_apply<double><<<grid_for(c, c->nnz, 256), 256, 0, c->st>>>(c->A64.p, c->nnz, c->B.p, c->neq, c->ks.p);
+    k_scale_apply<double><<<grid_for(c, c->nnz, 256), 256, 0, rg_counted(c)>>>(c->A64.p, c->nnz, c->B.p, c->neq, c->ks.p);
   else
-    k_scale_apply<float><<<grid_for(c, c->nnz, 256), 256, 0, c->st>>>(c->A32.p, c->nnz, c->B.p, c->neq, c->ks.p);
+    k_scale_apply<float><<<grid_for(c, c->nnz, 256), 256, 0, rg_counted(c)>>>(c->A32.p, c->nnz, c->B.p, c->neq, c->ks.p);
+  c->d2h_bytes += sizeof(KrylovScalars);
   cudaError_t e = cudaMemcpyAsync(c->ks_host, c->ks.p, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, c->st);
   if (e != cudaSuccess) return e;
   e = cudaStreamSynchronize(c->st);
@@ -815,7 +816,7 @@ static cudaError_t launch_factor_t(rg_ctx* c, const MT* A, MT* LU) {
   e = cudaMemcpyAsync(LU, A, c->nnz * sizeof(MT), cudaMemcpyDeviceToDevice, c->st);
   if (e != cudaSuccess) return e;
   void* args[] = {&n, &rp, &cl, &A, &LU, &lp, &lpos, &ff, &ep, &err};
-  return cudaLaunchCooperativeKernel((void*)k_factor<MT, WARPS>, blocks, WARPS * 32, args, 0, c->st);
+  return cudaLaunchCooperativeKernel((void*)k_factor<MT, WARPS>, blocks, WARPS * 32, args, 0, rg_counted(c));
 }
 
 template <class MT, int WARPS>
@@ -838,7 +839,7 @@ static cudaError_t launch_factor_level_t(rg_ctx* c, const MT* A, MT* LU) {
   const int* lspos = c->lsort_pos.p;
   int* err = c->dev_err.p;
   void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &err};
-  return cudaLaunchCooperativeKernel((void*)k_factor_level<MT, WARPS>, blocks, WARPS * 32, args, 0, c->st);
+  return cudaLaunchCooperativeKernel((void*)k_factor_level<MT, WARPS>, blocks, WARPS * 32, args, 0, rg_counted(c));
 }
 
 cudaError_t launch_factor(rg_ctx* c) {
@@ -872,11 +873,11 @@ static cudaError_t launch_factor_level2_t(rg_ctx* c, const MT* A, MT* LU) {
   const short* fm = c->fmap.p;
   int* err = c->dev_err.p;
   void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &lscol, &fo, &fm, &err};
-  return cudaLaunchCooperativeKernel((void*)k_factor_level2<MT, WARPS, STAGE>, blocks, WARPS * 32, args, 0, c->st);
+  return cudaLaunchCooperativeKernel((void*)k_factor_level2<MT, WARPS, STAGE>, blocks, WARPS * 32, args, 0, rg_counted(c));
 }
 
 cudaError_t launch_build_fmap(rg_ctx* c) {
-  k_build_fmap<<<c->num_sms * 4, 256, 0, c->st>>>(c->neq, c->rowptr.p, c->col.p, c->lsort_ptr.p, c->lsort_pos.p,
+  k_build_fmap<<<c->num_sms * 4, 256, 0, rg_counted(c)>>>(c->neq, c->rowptr.p, c->col.p, c->lsort_ptr.p, c->lsort_pos.p,
                                                    c->fmap_off.p, c->fmap.p);
   return cudaGetLastError();
 }
@@ -896,10 +897,10 @@ cudaError_t launch_split(rg_ctx* c) {
   int nl = (int)c->Lcol.n, nu = (int)c->Ucol.n;
   int g = grid_for(c, c->nnz, 256);
   if (c->prec == RG_PREC_FP64)
-    k_split<double><<<g, 256, 0, c->st>>>(c->neq, c->rowptr.p, c->LU64.p, nl, c->Lsrc.p, c->Lv64.p, nu, c->Usrc.p,
+    k_split<double><<<g, 256, 0, rg_counted(c)>>>(c->neq, c->rowptr.p, c->LU64.p, nl, c->Lsrc.p, c->Lv64.p, nu, c->Usrc.p,
                                           c->Uv64.p, c->Dv64.p);
   else
-    k_split<float><<<g, 256, 0, c->st>>>(c->neq, c->rowptr.p, c->LU32.p, nl, c->Lsrc.p, c->Lv32.p, nu, c->Usrc.p,
+    k_split<float><<<g, 256, 0, rg_counted(c)>>>(c->neq, c->rowptr.p, c->LU32.p, nl, c->Lsrc.p, c->Lv32.p, nu, c->Usrc.p,
                                          c->Uv32.p, c->Dv32.p);
   return cudaGetLastError();
 }
@@ -924,7 +925,7 @@ static cudaError_t launch_trsv_t(rg_ctx* c, const MT* val, const MT* diag, const
   const int* cl = LOWER ? c->Lcol.p : c->Ucol.p;
   int* err = c->dev_err.p;
   void* args[] = {&n, &ptr, &cl, &val, &diag, &b, &x, &err, &ks};
-  return cudaLaunchCooperativeKernel((void*)k_trsv<VT, MT, LOWER, W>, blocks, W * 32, args, 0, c->st);
+  return cudaLaunchCooperativeKernel((void*)k_trsv<VT, MT, LOWER, W>, blocks, W * 32, args, 0, rg_counted(c));
 }
 
 // y = M^-1 b with w as the intermediate; w and y must hold sentinels on entry
@@ -938,7 +939,9 @@ static cudaError_t ilu_apply_t(rg_ctx* c, const MT* Lv, const MT* Uv, const MT* 
 
 template <class VT, class MT, class AT, int ND>
 static void spmv_t(rg_ctx* c, const MT* A, const VT* x, VT* r, const VT* d1, int nb, const KrylovScalars* ks) {
-  k_spmv<VT, MT, AT, ND><<<nb, 256, 0, c->st>>>(c->neq, c->rowptr.p, c->col.p, A, x, r, d1, c->partial.p, ks);
+  prof_begin(c, RG_PROF_SPMV);
+  k_spmv<VT, MT, AT, ND><<<nb, 256, 0, rg_counted(c)>>>(c->neq, c->rowptr.p, c->col.p, A, x, r, d1, c->partial.p, ks);
+  prof_end(c);
 }
 
 cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r) {
@@ -953,8 +956,8 @@ cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r) {
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x) {
   if (c->use_wave && c->prec != RG_PREC_MIXED) return launch_wave_solve(c, true, b, c->tmp.p, x, nullptr);
   int nb = grid_for(c, c->neq, 256);
-  k_fill_sentinel<double><<<nb, 256, 0, c->st>>>(c->tmp.p, c->neq);
-  k_fill_sentinel<double><<<nb, 256, 0, c->st>>>(x, c->neq);
+  k_fill_sentinel<double><<<nb, 256, 0, rg_counted(c)>>>(c->tmp.p, c->neq);
+  k_fill_sentinel<double><<<nb, 256, 0, rg_counted(c)>>>(x, c->neq);
   if (c->prec == RG_PREC_FP64)
     return ilu_apply_t<double, double>(c, c->Lv64.p, c->Uv64.p, c->Dv64.p, b, c->tmp.p, x, nullptr);
   return ilu_apply_t<double, float>(c, c->Lv32.p, c->Uv32.p, c->Dv32.p, b, c->tmp.p, x, nullptr);
@@ -979,36 +982,37 @@ static rg_status bicgstab_t(rg_ctx* c, const MT* A, const MT* Lv, const MT* Uv, 
     e = (x);                                         \
     if (e != cudaSuccess) return rg_cuda(c, e, #x);  \
   } while (0)
-  k_fill<VT><<<nb, 256, 0, c->st>>>(x, n, (VT)0);
-  k_fill<VT><<<nb, 256, 0, c->st>>>(xm, n, (VT)0);
-  k_fill<VT><<<nb, 256, 0, c->st>>>(ti, n, (VT)0);   // t_ = A x = 0 for x = 0
-  k_bicg_start<VT><<<nb, 256, 0, c->st>>>(n, b, ti, r0, ri, pi, vi, part);
-  k_bicg_init<<<1, 256, 0, c->st>>>(part, nb, ks);
+  k_fill<VT><<<nb, 256, 0, rg_counted(c)>>>(x, n, (VT)0);
+  k_fill<VT><<<nb, 256, 0, rg_counted(c)>>>(xm, n, (VT)0);
+  k_fill<VT><<<nb, 256, 0, rg_counted(c)>>>(ti, n, (VT)0);   // t_ = A x = 0 for x = 0
+  k_bicg_start<VT><<<nb, 256, 0, rg_counted(c)>>>(n, b, ti, r0, ri, pi, vi, part);
+  k_bicg_init<<<1, 256, 0, rg_counted(c)>>>(part, nb, ks);
   CK(cudaGetLastError());
   int it = 0;
   rg_status st = RG_OK;
   for (;;) {
-    k_bicg_beta<<<1, 1, 0, c->st>>>(ks);
-    k_bicg_p<VT><<<nb, 256, 0, c->st>>>(n, pi, ri, vi, ks, w, yi);
+    k_bicg_beta<<<1, 1, 0, rg_counted(c)>>>(ks);
+    k_bicg_p<VT><<<nb, 256, 0, rg_counted(c)>>>(n, pi, ri, vi, ks, w, yi);
     if (c->use_wave)
       CK(launch_wave_solve(c, sizeof(VT) == 8, pi, w, yi, nullptr));
     else
       CK((ilu_apply_t<VT, MT>(c, Lv, Uv, Dv, pi, w, yi, nullptr)));
     spmv_t<VT, MT, AT, 1>(c, A, yi, vi, r0, nbs, nullptr);
-    k_bicg_alfa<<<1, 256, 0, c->st>>>(part, nbs, ks);
-    k_bicg_r1<VT><<<nb, 256, 0, c->st>>>(n, ri, vi, ks, part);
-    k_bicg_diff<<<1, 256, 0, c->st>>>(part, nb, ks, maxDiff, maxIter);
-    k_bicg_xm<VT><<<nb, 256, 0, c->st>>>(n, x, yi, xm, x, ks);
+    k_bicg_alfa<<<1, 256, 0, rg_counted(c)>>>(part, nbs, ks);
+    k_bicg_r1<VT><<<nb, 256, 0, rg_counted(c)>>>(n, ri, vi, ks, part);
+    k_bicg_diff<<<1, 256, 0, rg_counted(c)>>>(part, nb, ks, maxDiff, maxIter);
+    k_bicg_xm<VT><<<nb, 256, 0, rg_counted(c)>>>(n, x, yi, xm, x, ks);
     // second half, skipped on the device once converged or out of iterations
-    k_fill_sentinel_if<VT><<<nb, 256, 0, c->st>>>(w, zi, n, ks);
+    k_fill_sentinel_if<VT><<<nb, 256, 0, rg_counted(c)>>>(w, zi, n, ks);
     if (c->use_wave)
       CK(launch_wave_solve(c, sizeof(VT) == 8, ri, w, zi, ks));
     else
       CK((ilu_apply_t<VT, MT>(c, Lv, Uv, Dv, ri, w, zi, ks)));
     spmv_t<VT, MT, AT, 2>(c, A, zi, ti, ri, nbs, ks);
-    k_bicg_omega<<<1, 256, 0, c->st>>>(part, nbs, ks);
-    k_bicg_x<VT><<<nb, 256, 0, c->st>>>(n, x, yi, zi, ri, ti, r0, ks, part);
-    k_fin_t1<<<1, 256, 0, c->st>>>(part, nb, ks);
+    k_bicg_omega<<<1, 256, 0, rg_counted(c)>>>(part, nbs, ks);
+    k_bicg_x<VT><<<nb, 256, 0, rg_counted(c)>>>(n, x, yi, zi, ri, ti, r0, ks, part);
+    k_fin_t1<<<1, 256, 0, rg_counted(c)>>>(part, nb, ks);
+    c->d2h_bytes += sizeof(KrylovScalars);
     CK(cudaMemcpyAsync(c->ks_host, ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     it = c->ks_host->it;
@@ -1032,8 +1036,8 @@ static rg_status bicgstab_t(rg_ctx* c, const MT* A, const MT* Lv, const MT* Uv, 
     if (fabs(c->ks_host->t1) < 1.0e-30) {
       // restart (Bicgstab.cpp:174-199): r = r0 = b - A x, p = v = 0, scalars reset
       spmv_t<VT, MT, AT, 0>(c, A, x, ti, nullptr, nbs, nullptr);
-      k_bicg_restart<VT><<<nb, 256, 0, c->st>>>(n, b, ti, r0, ri, pi, vi, part);
-      k_bicg_restart_fin<<<1, 256, 0, c->st>>>(part, nb, ks);
+      k_bicg_restart<VT><<<nb, 256, 0, rg_counted(c)>>>(n, b, ti, r0, ri, pi, vi, part);
+      k_bicg_restart_fin<<<1, 256, 0, rg_counted(c)>>>(part, nb, ks);
       CK(cudaGetLastError());
     }
   }
@@ -1058,14 +1062,15 @@ rg_status run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, doubl
   const int nb = grid_for(c, n, 256);
   const int nbs = grid_for(c, n * 16ll, 256);
   cudaError_t e;
-  k_fill<double><<<nb, 256, 0, c->st>>>(c->X.p, n, 0.0);
+  k_fill<double><<<nb, 256, 0, rg_counted(c)>>>(c->X.p, n, 0.0);
   double bnorm = -1.0, last = 1.0;
   int total = 0;
   rg_status st = RG_NOT_CONVERGED;
   for (int refine = 0; refine < 12; refine++) {
     spmv_t<double, float, double, 0>(c, c->A32.p, c->X.p, c->tt.p, nullptr, nbs, nullptr);
-    k_resid<<<nb, 256, 0, c->st>>>(n, c->B.p, c->tt.p, c->f_b.p, c->partial.p);
-    k_fin_to<<<1, 256, 0, c->st>>>(c->partial.p, nb, &c->ks.p->t2);
+    k_resid<<<nb, 256, 0, rg_counted(c)>>>(n, c->B.p, c->tt.p, c->f_b.p, c->partial.p);
+    k_fin_to<<<1, 256, 0, rg_counted(c)>>>(c->partial.p, nb, &c->ks.p->t2);
+    c->d2h_bytes += sizeof(KrylovScalars);
     e = cudaMemcpyAsync(c->ks_host, c->ks.p, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     if (e != cudaSuccess) return rg_cuda(c, e, "mixed residual");
@@ -1089,7 +1094,7 @@ rg_status run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, doubl
                                                    &a2);
     total += its;
     if (s2 != RG_OK && s2 != RG_NOT_CONVERGED) return s2;
-    k_add_f<<<nb, 256, 0, c->st>>>(n, c->f_x.p, c->X.p);
+    k_add_f<<<nb, 256, 0, rg_counted(c)>>>(n, c->f_x.p, c->X.p);
     e = cudaGetLastError();
     if (e != cudaSuccess) return rg_cuda(c, e, "mixed update");
   }

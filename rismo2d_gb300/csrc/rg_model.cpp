@@ -951,6 +951,40 @@ rg_status rg_sim_get_boundary(rg_sim* s, int* nflag, int* bckind, double* rot4, 
   return RG_OK;
 }
 
+rg_status rg_sim_get_model(rg_sim* s, int* ne, int* elem_nodes, int* elem_nnd, int* elem_flag, double* elem_vt,
+                           double* niox, double* nioy) {
+  if (!s) return RG_ERR_ARG;
+  const size_t nme = s->melems.size();
+  if (ne) *ne = (int)nme;
+  for (size_t e = 0; e < nme; e++) {
+    const int me = s->melems[e];
+    int nd[6] = {-1, -1, -1, -1, -1, -1}, nnd, fl;
+    double vt;
+    if (me >= 0) {
+      for (int i = 0; i < 6; i++) nd[i] = s->en[6 * me + i];
+      nnd = 6;
+      fl = (int)s->eflag[me];
+      vt = s->en_vt[me];
+    } else {
+      const BElem& b = s->bel[-1 - me];
+      for (int i = 0; i < 3; i++) nd[i] = b.nd[i];
+      nnd = 3;
+      fl = (int)b.flag;
+      vt = s->en_vt[b.region];
+    }
+    if (elem_nodes)
+      for (int i = 0; i < 6; i++) elem_nodes[6 * e + i] = nd[i];
+    if (elem_nnd) elem_nnd[e] = nnd;
+    if (elem_flag) elem_flag[e] = fl;
+    if (elem_vt) elem_vt[e] = vt;
+  }
+  for (int n = 0; n < s->np; n++) {
+    if (niox) niox[n] = s->niox[n];
+    if (nioy) nioy[n] = s->nioy[n];
+  }
+  return RG_OK;
+}
+
 rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg_step_report* rep) {
   if (!s || !ctl || !s->have_state || dt <= 0.0) return RG_ERR_ARG;
   if (!s->ctx) return sfail(s, RG_ERR_ARG, "rg_sim_step: created without a GPU context");

@@ -212,7 +212,7 @@ static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, con
   int nb = (n + 255) / 256;
   if (nb > c->num_sms * 4) nb = c->num_sms * 4;
   VT* blev = reinterpret_cast<VT*>(wd.blev.p);
-  k_gather_lev<VT><<<nb, 256, 0, c->st>>>(n, wd.order.p, wd.bidx.p, b, blev, ks);
+  k_gather_lev<VT><<<nb, 256, 0, rg_counted(c)>>>(n, wd.order.p, wd.bidx.p, b, blev, ks);
   const size_t smem = (RING + PIN) * sizeof(VT) + 3 * (size_t)wd.stage_bytes + 3 * (size_t)wd.bstage_bytes;
   static bool attr_done[2][2] = {{false, false}, {false, false}};
   bool& done = attr_done[sizeof(VT) == 8][LOWER];
@@ -223,21 +223,28 @@ static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, con
     if (e != cudaSuccess) return e;
     done = true;
   }
-  k_trsv_wave<VT, LOWER, RING, PIN><<<1, kThreads, smem, c->st>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, blev, x,
+  k_trsv_wave<VT, LOWER, RING, PIN><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, blev, x,
                                                              wd.stage_bytes, wd.bstage_bytes, c->dev_err.p, ks);
   return cudaGetLastError();
 }
 
 cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void* y, const KrylovScalars* ks) {
-  cudaError_t e;
-  if (dbl) {
-    e = launch_wave_t<double, true>(c, c->waveL, (const double*)b, (double*)w, ks);
-    if (e != cudaSuccess) return e;
-    return launch_wave_t<double, false>(c, c->waveU, (const double*)w, (double*)y, ks);
-  }
-  e = launch_wave_t<float, true>(c, c->waveL, (const float*)b, (float*)w, ks);
+  cudaError_t e = prof_begin(c, RG_PROF_TRSV);
   if (e != cudaSuccess) return e;
-  return launch_wave_t<float, false>(c, c->waveU, (const float*)w, (float*)y, ks);
+  if (dbl)
+    e = launch_wave_t<double, true>(c, c->waveL, (const double*)b, (double*)w, ks);
+  else
+    e = launch_wave_t<float, true>(c, c->waveL, (const float*)b, (float*)w, ks);
+  if (e != cudaSuccess) return e;
+  e = prof_end(c);
+  if (e == cudaSuccess) e = prof_begin(c, RG_PROF_TRSV);
+  if (e != cudaSuccess) return e;
+  if (dbl)
+    e = launch_wave_t<double, false>(c, c->waveU, (const double*)w, (double*)y, ks);
+  else
+    e = launch_wave_t<float, false>(c, c->waveU, (const float*)w, (float*)y, ks);
+  if (e != cudaSuccess) return e;
+  return prof_end(c);
 }
 
 // pack the current factors into both images
@@ -245,15 +252,15 @@ cudaError_t launch_wave_pack(rg_ctx* c) {
   for (WaveDev* wd : {&c->waveL, &c->waveU}) {
     int nb = (int)std::min<long long>((wd->nent + 255) / 256 + 1, (long long)c->num_sms * 8);
     if (c->prec == RG_PREC_FP64)
-      k_pack_wave<double, double><<<nb, 256, 0, c->st>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,
+      k_pack_wave<double, double><<<nb, 256, 0, rg_counted(c)>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,
                                                          (int)wd->ndiag, wd->diag_dst.p, wd->diag_src.p,
                                                          c->LU64.p, wd->img.p);
     else if (c->prec == RG_PREC_REF32)
-      k_pack_wave<float, double><<<nb, 256, 0, c->st>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,
+      k_pack_wave<float, double><<<nb, 256, 0, rg_counted(c)>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,
                                                         (int)wd->ndiag, wd->diag_dst.p, wd->diag_src.p, c->LU32.p,
                                                         wd->img.p);
     else
-      k_pack_wave<float, float><<<nb, 256, 0, c->st>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,
+      k_pack_wave<float, float><<<nb, 256, 0, rg_counted(c)>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,
                                                        (int)wd->ndiag, wd->diag_dst.p, wd->diag_src.p, c->LU32.p,
                                                        wd->img.p);
   }

@@ -102,6 +102,13 @@ def channel(nx: int = 50, ny: int = 10, length: float = 1000.0, width: float = 1
                 meta=dict(kind="channel", nx=nx, ny=ny, Q=Q, S_out=S_out, steady=True))
 
 
+def sin2_hydrograph(Q0: float = 300.0, dQ: float = 500.0, period: float = 7200.0, t_end: float = 7200.0,
+                    every: float = 600.0, S: float = 4.0) -> list:
+    """QTINLET table of Q(t) = Q0 + dQ sin^2(pi t / period), one row per `every` seconds."""
+    ts = np.arange(0.0, t_end + 0.5 * every, every)
+    return [(float(t), Q0 + dQ * np.sin(np.pi * t / period) ** 2, S) for t in ts]
+
+
 def meander(nx: int = 1266, ny: int = 79, length: float = 10000.0, amplitude: float = 80.0,
             wavelength: float = 400.0, channel_width: float = 60.0, channel_depth: float = 4.0,
             plain_width: float = 200.0, plain_rise: float = 1.0, valley_slope: float = 5.0e-4,

@@ -205,6 +205,53 @@ class Simulation:
         self.lib.rg_sim_get_pattern(self.ptr, p(index))
         return dict(neq=neq.value, eqno=eqno.reshape(-1, 3), width=width, index=index)
 
+    def model(self) -> dict:
+        """Model element list and open-boundary normals of the last model build."""
+        ne = C.c_int()
+        self.lib.rg_sim_get_model(self.ptr, C.byref(ne), None, None, None, None, None, None)
+        m = ne.value
+        out = dict(elem_nodes=np.zeros((m, 6), np.int32), elem_nnd=np.zeros(m, np.int32),
+                   elem_flag=np.zeros(m, np.int32), elem_vt=np.zeros(m), niox=np.zeros(self.np),
+                   nioy=np.zeros(self.np))
+        st = self.lib.rg_sim_get_model(self.ptr, None, p(out["elem_nodes"]), p(out["elem_nnd"]),
+                                       p(out["elem_flag"]), p(out["elem_vt"]), p(out["niox"]), p(out["nioy"]))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_get_model: " + self._err())
+        return out
+
+    # -- the GPU context: structure, copy counters, per-kernel device time ----
+    def context(self) -> C.c_void_p:
+        self.lib.rg_sim_context.restype = C.c_void_p
+        return C.c_void_p(self.lib.rg_sim_context(self.ptr))
+
+    def stats(self) -> np.ndarray:
+        out = np.zeros(15, np.int64)
+        self.lib.rg_get_stats(self.context(), p(out), C.c_int(15))
+        return out
+
+    def profile(self, enable: bool, reset: bool = True):
+        st = self.lib.rg_profile(self.context(), C.c_int(1 if enable else 0), C.c_int(1 if reset else 0))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_profile")
+
+    def profile_read(self) -> dict:
+        out = np.zeros(8)
+        self.lib.rg_profile_read(self.context(), p(out), C.c_int(8))
+        names = ("trsv", "spmv", "factor", "assemble")
+        return {k: (int(out[2 * i]), float(out[2 * i + 1])) for i, k in enumerate(names)}
+
+    def event_record(self, slot: int):
+        st = self.lib.rg_event_record(self.context(), C.c_int(slot))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_event_record")
+
+    def event_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        st = self.lib.rg_event_elapsed(self.context(), C.c_int(a), C.c_int(b), C.byref(ms))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_event_elapsed")
+        return ms.value
+
     def boundary(self) -> dict:
         out = dict(nflag=np.zeros(self.np, np.int32), bckind=np.zeros(self.np, np.int32),
                    rot4=np.zeros((self.np, 4)), bcU=np.zeros(self.np), bcS=np.zeros(self.np))
