@@ -158,7 +158,7 @@ def l2_flush(buf):
 
 
 def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, clocks: Clocks | None, dist: Dist,
-            flush_buf):
+            flush_buf, max_newton: int = 0):
     """W warm-up and K timed time steps through Simulation.step; per-step device time by
     CUDA events on the library's stream, host wall time of step + state download."""
     import torch
@@ -169,7 +169,8 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
     t = 0.0
     reps = []
     for _ in range(warmup):
-        reps.append(sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL))
+        reps.append(sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL,
+                             max_newton=max_newton))
         t += STEP_DT
     st0 = sim.stats()
     if profile:
@@ -185,7 +186,7 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
         l2_flush(flush_buf)
         h0 = time.perf_counter()
         sim.event_record(0)
-        rep = sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL)
+        rep = sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL, max_newton=max_newton)
         sim.event_record(1)
         state = sim.get_state()               # result to host memory (numpy)
         h1 = time.perf_counter()
@@ -341,7 +342,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the plain FP64 comparison (0: skip)")
-    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU solver sampling")
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU solver sampling (0: skip)")
+    ap.add_argument("--max-newton", type=int, default=0,
+                    help="cap on Newton iterations per step, for short profiling runs only (0: none; a capped "
+                         "run is not a benchmark result)")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -377,7 +381,7 @@ def main():
     flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}")   # 256 MiB > L2
     from rismo2d_gb300 import _lib
     clocks = Clocks(device)
-    mixed = run_gpu(_lib.PREC_MIXED, warmup, args.steps, device, True, clocks, dist, flush_buf)
+    mixed = run_gpu(_lib.PREC_MIXED, warmup, args.steps, device, True, clocks, dist, flush_buf, args.max_newton)
     k = args.steps
     dev_s = sum(mixed["dev_ms"]) / 1e3
     dev_s_max = dist.max(dev_s)
@@ -389,7 +393,7 @@ def main():
     fp64 = None
     if args.fp64_steps > 0:
         kf = min(args.fp64_steps, k)
-        f = run_gpu(_lib.PREC_FP64, warmup, kf, device, False, None, dist, flush_buf)
+        f = run_gpu(_lib.PREC_FP64, warmup, kf, device, False, None, dist, flush_buf, args.max_newton)
         fs = sum(f["dev_ms"]) / 1e3 / kf
         errs = []
         for j in range(kf):
@@ -406,7 +410,7 @@ def main():
                 "mixed_speedup": round(fs / (dev_s / k), 3),
                 "mixed_vs_fp64_max_rel_err": errs}
     cpu = None
-    if dist.rank == 0:
+    if dist.rank == 0 and args.cpu_budget > 0:
         nps = fp64["newton_per_step"] if fp64 else statistics.mean(newton)
         kps = fp64["krylov_per_step"] if fp64 else statistics.mean(krylov)
         cpu = cpu_baseline(args.cpu_budget, nps, kps)
@@ -435,6 +439,8 @@ def main():
                 "gpu_launches": mixed["launches"],
                 "device_ms_by_kernel_class": {kk: [v[0], round(v[1], 2)] for kk, v in mixed["prof"].items()},
                 "roofline": roof, "cpu_baseline": cpu}
+        if args.max_newton:
+            line["profiling_case"] = f"Newton capped at {args.max_newton} per step: not a benchmark result"
         print(json.dumps(line), flush=True)
     dist.close()
     return 0
