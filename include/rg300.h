@@ -122,6 +122,27 @@ rg_status rg_ilu0_factor(rg_ctx* ctx, float* LU32_out, double* LU64_out);
 /* PRECO_ILU0::Solve (Preco_ilu0.cpp:497-980) of a host vector. */
 rg_status rg_ilu0_apply(rg_ctx* ctx, const double* B, double* X);
 
+/* PRECO_ILU0::Solve of a DEVICE vector, allocating nothing: x_dev = M^-1 b_dev
+ * with the resident factors, for callers that must not allocate during a
+ * solve (a caller that pre-plans all device memory, or one whose loop cannot
+ * take the implicit synchronisation of cudaMalloc/cudaFree).  No counterpart
+ * in the reference.
+ *  - The intermediate vector of the two triangular solves is a fixed
+ *    file-scope device array of RG_NOALLOC_MAX_EQ doubles (2 MiB); a system
+ *    with more equations is rejected with RG_ERR_ARG (use rg_ilu0_apply).
+ *    Nothing in that array has to start at zero.
+ *  - The first call on a device looks up the array's address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture
+ *    begins on the device.
+ *  - All contexts of a process share the one array per device: calls that
+ *    overlap in time on the same device (two host threads, or two contexts)
+ *    race on it and must be serialised by the caller.
+ *  - b_dev and x_dev hold neq doubles each; the call runs on the context's
+ *    stream and returns when the result is in x_dev, so b_dev must be
+ *    complete when the call is made. */
+#define RG_NOALLOC_MAX_EQ (1 << 18)
+rg_status rg_ilu0_apply_dev_noalloc(rg_ctx* ctx, const double* b_dev, double* x_dev);
+
 /* CRSMAT::MulVec (CRSMat.cpp:466-496) of a host vector with the resident matrix. */
 rg_status rg_spmv(rg_ctx* ctx, const double* x, double* r);
 

@@ -35,7 +35,8 @@ EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pat
            "rg_sim_step", "rg_sim_prepare_iteration", "rg_sim_get_numbering", "rg_sim_get_pattern",
            "rg_sim_get_boundary", "rg_set_elements", "rg_set_old", "rg_get_dt", "rg_timegrad",
            "rg_zero_velocity", "rg_sim_dry_rewet", "rg_get_stats", "rg_event_record", "rg_event_elapsed",
-           "rg_sim_context", "rg_profile", "rg_profile_read", "rg_sim_get_model"]
+           "rg_sim_context", "rg_profile", "rg_profile_read", "rg_sim_get_model",
+           "rg_ilu0_apply_dev_noalloc"]
 
 
 class RgMesh(C.Structure):

@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librg300.so")
-SOURCES = ["rg_assemble.cu", "rg_linalg.cu", "rg_trsv.cu", "rg_api.cu", "rg_model.cpp", "rg_wave_layout.cpp"]
+SOURCES = ["rg_assemble.cu", "rg_linalg.cu", "rg_trsv.cu", "rg_api.cu", "rg_noalloc.cu", "rg_model.cpp",
+           "rg_wave_layout.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

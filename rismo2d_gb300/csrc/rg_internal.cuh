@@ -240,6 +240,7 @@ cudaError_t launch_build_fmap(rg_ctx* c);
 cudaError_t launch_split(rg_ctx* c);
 cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r);
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x);
+cudaError_t launch_ilu_apply_w(rg_ctx* c, const double* b, double* w, double* x);
 rg_status   run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, double* acc);
 cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void* y, const KrylovScalars* ks);
 cudaError_t launch_wave_pack(rg_ctx* c);

@@ -1102,3 +1102,15 @@ rg_status run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, doubl
   if (acc) *acc = last;
   return st;
 }
+
+// y = M^-1 b on double vectors with a caller-chosen intermediate w (n values):
+// the same kernels as launch_ilu_apply_d, which uses the context's own vector
+cudaError_t launch_ilu_apply_w(rg_ctx* c, const double* b, double* w, double* x) {
+  if (c->use_wave && c->prec != RG_PREC_MIXED) return launch_wave_solve(c, true, b, w, x, nullptr);
+  int nb = grid_for(c, c->neq, 256);
+  k_fill_sentinel<double><<<nb, 256, 0, rg_counted(c)>>>(w, c->neq);
+  k_fill_sentinel<double><<<nb, 256, 0, rg_counted(c)>>>(x, c->neq);
+  if (c->prec == RG_PREC_FP64)
+    return ilu_apply_t<double, double>(c, c->Lv64.p, c->Uv64.p, c->Dv64.p, b, w, x, nullptr);
+  return ilu_apply_t<double, float>(c, c->Lv32.p, c->Uv32.p, c->Dv32.p, b, w, x, nullptr);
+}
