@@ -513,13 +513,21 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
   // schedule of the factorisation
   {
     const int vtb = (c->prec == RG_PREC_MIXED) ? 4 : 8;
-    const int stage_cap = (vtb == 8) ? kWaveStage64 : kWaveStage32;
-    const int bstage_cap = (vtb == 8) ? kWaveBStage64 : kWaveBStage32;
+    // stages: what the shared-memory budget leaves after the ring and pinned slots
+    const int nst = (vtb == 8) ? kWaveStages64 : kWaveStages32;
+    const int stage_cap = (int)(((kWaveSmem - (long long)(kWaveRing + kWavePin) * vtb) / nst) & ~255ll);
     std::vector<int> diag_pos(rowptr.begin(), rowptr.end() - 1);
+    // threads per row (RG_WAVE_LANES = 1, 2 or 4 overrides it for the FP32 solve, for tuning)
+    int lanes = (vtb == 8) ? kWaveLanes64 : kWaveLanes32;
+    if (const char* e = getenv("RG_WAVE_LANES"))
+      if (vtb == 4 && (atoi(e) == 1 || atoi(e) == 2 || atoi(e) == 4)) lanes = atoi(e);
+    // rows per chunk: one per consumer thread group (RG_WAVE_ROWS lowers the cap, for tuning)
+    int rows_cap = kWaveRows / lanes;
+    if (const char* e = getenv("RG_WAVE_ROWS")) rows_cap = std::max(32, std::min(rows_cap, atoi(e)));
     WaveLayout wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, kWavePin, stage_cap,
-                                      bstage_cap);
+                                      rows_cap, lanes);
     WaveLayout wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, kWavePin, stage_cap,
-                                      bstage_cap);
+                                      rows_cap, lanes);
     for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {
       WaveLayout& w = *pr.first;
       WaveDev& d = *pr.second;
@@ -531,16 +539,21 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
       TRY(upload(c, d.ent_dst, w.ent_dst.data(), std::max<size_t>(w.ent_dst.size(), 1)));
       TRY(upload(c, d.diag_src, w.diag_src.data(), std::max<size_t>(w.diag_src.size(), 1)));
       TRY(upload(c, d.diag_dst, w.diag_dst.data(), std::max<size_t>(w.diag_dst.size(), 1)));
-      TRY(d.blev.alloc((size_t)w.blev_len * vtb + 64));
       d.nchunks = (long long)w.chunks.size();
       d.nent = (long long)w.ent_src.size();
       d.ndiag = (long long)w.diag_src.size();
       d.stage_bytes = stage_cap;
-      d.bstage_bytes = bstage_cap;
+      d.lanes = lanes;
       d.depth = w.depth;
       d.ring_misses = w.ring_misses;
+      d.max_chunk_bytes = 0;
+      for (const WaveChunk& ch : w.chunks) d.max_chunk_bytes = std::max(d.max_chunk_bytes, ch.img_bytes);
       TRY(cudaStreamSynchronize(c->st));   // host images are freed at scope end
     }
+    // a row too wide for one stage (never with P2 triangles: at most ~45 entries)
+    // leaves the solves to the dependency-driven kernels
+    c->use_wave = (c->waveL.max_chunk_bytes <= stage_cap && c->waveU.max_chunk_bytes <= stage_cap) ? 1 : 0;
+    if (const char* e = getenv("RG_NO_WAVE")) c->use_wave = atoi(e) ? 0 : c->use_wave;
     // factor schedule: rows grouped by L level (the L solve's level order)
     std::vector<int> lev(neq, 0), fptr;
     int nlev = 0;

@@ -53,32 +53,38 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
-// level-ordered chunk layout of one triangular factor (rg_trsv.cu)
+// level-ordered chunk layout of one triangular factor (rg_trsv.cu).  A chunk
+// image is meta[m] (int4: row, entry count, byte offset of its warp slice,
+// pinned slot or -1) | b[m] | diag[m] (U solve) | warp slices.  A slice holds
+// the entries of 32/G rows (G threads per row) column by column: column t has
+// 32 source slots (int32) then 32 values, lane l = G*(row in slice) + g
+// holding the row's entry j = G*t + g, so lane l reads its entry at
+// slice + t*32*(4+sizeof(VT)) + 4*l (source) and + 128 + sizeof(VT)*l (value).
 struct WaveChunk {
   long long img_off;   // byte offset of the chunk image (16-aligned)
   int img_bytes;       // multiple of 16
   int nrows;
-  int nent;
-  int diag_off;        // byte offsets inside the image: diagonal (U solve), values, sources
-  int val_off;
-  int src_off;
-  int b_off;           // element offset into the level-ordered, padded right-hand side
-  int b_bytes;         // multiple of 16
   int pos0;            // level-order position of the chunk's first row
+  int b_off;           // byte offsets inside the image: right-hand side, diagonal (U solve)
+  int diag_off;
   int pad;
 };
-// shared-memory budget of the wavefront solve (per precision of the vectors):
-// ring and pinned slots, three image stages, three right-hand-side stages
+constexpr int kWaveSlice = 32;      // rows per warp slice
+constexpr int kWaveThreads = 544;   // one CTA: 16 consumer warps + 1 producer warp
+constexpr int kWaveRows = kWaveThreads - 32;   // rows per chunk at most (one per consumer thread)
+constexpr int kWaveMaxStages = 8;
+// shared-memory stages in flight: the double ring leaves room for two large ones
+constexpr int kWaveStages32 = 3, kWaveStages64 = 2;
+// shared-memory ring of solved values and pinned slots for far sources
 constexpr int kWaveRing = 16384;
 constexpr int kWavePin = 4096;
-constexpr int kWaveStage32 = 40960, kWaveBStage32 = 4096;   // float: 64+16+120+12 KB
-constexpr int kWaveStage64 = 20480, kWaveBStage64 = 2048;   // double: 128+32+60+6 KB
+// dynamic shared memory available to the wavefront kernel
+constexpr int kWaveSmem = 232448 - 2048;
 struct WaveLayout {
   int n = 0, depth = 0;
   std::vector<WaveChunk> chunks;
   std::vector<unsigned char> img_host;
   long long img_bytes = 0;
-  int blev_len = 0;
   std::vector<int> order, bidx, ent_src, diag_src;
   std::vector<long long> ent_dst, diag_dst;
   long long ring_misses = 0;
@@ -86,10 +92,15 @@ struct WaveLayout {
 };
 // ring: shared-memory ring slots; pin: fixed slots for sources read from
 // farther back than the ring reaches (src encoding: [0, ring) ring slot,
-// [ring, ring + pin) pinned slot, negative: -(row + 1) in global memory)
+// [ring, ring + pin) pinned slot, negative: -(row + 1) in global memory);
+// bidx[p]: element index (in units of the vector type) of the right-hand side
+// slot of level-order position p inside the image
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
                              const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
-                             int vt_bytes, int ring, int pin, int stage_cap, int bstage_cap);
+                             int vt_bytes, int ring, int pin, int stage_cap, int rows_max, int lanes);
+// threads per row of the wavefront solves: one, i.e. the reference's summation
+// order (bit-identical for double vectors); 2 or 4 split long rows
+constexpr int kWaveLanes64 = 1, kWaveLanes32 = 1;
 
 // per-solve scalars kept on the device (BiCGStab state, reductions)
 struct KrylovScalars {
@@ -104,9 +115,8 @@ struct WaveDev {
   DBuf<WaveChunk> chunks;
   DBuf<int> order, bidx, ent_src, diag_src;
   DBuf<long long> ent_dst, diag_dst;
-  DBuf<unsigned char> blev;
   long long nchunks = 0, nent = 0, ndiag = 0;
-  int stage_bytes = 0, bstage_bytes = 0, depth = 0;
+  int stage_bytes = 0, lanes = 1, depth = 0, max_chunk_bytes = 0;
   long long ring_misses = 0;
   // level schedule of the factorisation (L levels)
   std::vector<int> lev_ptr;

@@ -5,15 +5,15 @@
 // The solves are latency-bound chains (a level holds a few hundred rows, the
 // depth is hundreds to thousands of levels), so the kernel keeps the whole
 // chain on one SM and takes global-memory latency off the critical path:
-//   * the rows of every level are packed host-side into a contiguous image
-//     {row meta, diagonal, (value, source) entries} padded to 16 bytes;
-//   * thread 0 streams the images of the next levels into a 3-stage shared
-//     memory buffer with cp.async.bulk (TMA bulk copies) completing on
-//     mbarriers, together with the right-hand side gathered into level order;
+//   * the rows of every level are packed host-side into a contiguous image per
+//     chunk (row meta, right-hand side, diagonal, warp slices of entries);
+//   * one producer thread streams the images of the next chunks into NST
+//     shared-memory stages with cp.async.bulk (TMA bulk copies) completing on
+//     mbarriers; the next chunk descriptor is loaded while it waits;
 //   * solution values live in a shared-memory ring indexed by level-order
-//     position; the host decides per entry whether its source is still in the
-//     ring (else it is read back from global memory);
-//   * levels are separated by __syncthreads.
+//     position, plus pinned slots for the most-read far sources; the host
+//     decides per entry where its source is (else it is read from global memory);
+//   * one consumer thread per row; chunks are separated by a named barrier.
 // Levels too large for a stage are split into consecutive chunks (rows of one
 // level do not depend on each other).  All waits are bounded.
 
@@ -24,9 +24,9 @@
 
 namespace {
 
-constexpr int kThreads = 1024;
-constexpr int kGroup = 4;                 // threads per row
+constexpr int kThreads = kWaveThreads;
 constexpr long long kMbarSpin = 1ll << 26;
+constexpr long long kDrainSpin = 1ll << 16;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -73,10 +73,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 // bounded wait on an mbarrier phase; false when the bound ran out
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, long long limit = kMbarSpin) {
   long long it = 0;
   while (!mbar_try_wait(bar, parity)) {
-    if (++it > kMbarSpin) return false;
+    if (++it > limit) return false;
   }
   return true;
 }
@@ -86,108 +86,185 @@ __device__ __forceinline__ void consumers_sync() {
 }
 
 // Warp-specialised wavefront solve: warp 31 (one elected lane) is the producer
-// that streams chunk images and right-hand sides into NST stages with
-// cp.async.bulk; warps 0..30 consume the stages in order, one dependency level
-// chunk at a time, synchronising on a named barrier between chunks.
-template <class VT, bool LOWER, int RING, int PIN>
+// that streams chunk images into NST shared-memory stages with cp.async.bulk;
+// warps 0..30 consume the stages in order, one dependency-level chunk at a
+// time, one row per thread, synchronising on a named barrier between chunks.
+//
+// Row r of a chunk is solved by consumer thread r: its entries sit in its warp
+// slice column by column, so the 32 lanes of a warp read consecutive words.
+// The sum runs over the row's entries in the factor's order with separately
+// rounded products and sums, as PRECO_ILU0::Solve does (Preco_ilu0.cpp:520-528
+// forward from b, 964-977 backward, then the division by the diagonal).
+template <class VT>
+__device__ __forceinline__ VT fmul(VT a, VT b);
+template <>
+__device__ __forceinline__ float fmul<float>(float a, float b) { return __fmul_rn(a, b); }
+template <>
+__device__ __forceinline__ double fmul<double>(double a, double b) { return __dmul_rn(a, b); }
+template <class VT>
+__device__ __forceinline__ VT fadd(VT a, VT b);
+template <>
+__device__ __forceinline__ float fadd<float>(float a, float b) { return __fadd_rn(a, b); }
+template <>
+__device__ __forceinline__ double fadd<double>(double a, double b) { return __dadd_rn(a, b); }
+
+// the solution value at source slot s: ring or pinned slot, or (FAR layouts
+// only) -(row + 1) for a row read back from global memory
+template <class VT, bool FAR>
+__device__ __forceinline__ VT source_value(const VT* vals, const VT* x, int s) {
+  if (FAR) return s >= 0 ? vals[s] : x[-s - 1];
+  return vals[s];
+}
+
+template <class VT, bool LOWER, int G, bool FAR>
 __global__ void __launch_bounds__(kThreads, 1)
     k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, const unsigned char* __restrict__ img,
-                const VT* __restrict__ blev, VT* __restrict__ x, int stage_bytes, int bstage_bytes, int* err,
-                const KrylovScalars* ks) {
+                VT* __restrict__ x, int stage_bytes, int* err, const KrylovScalars* ks) {
   if (ks && ks->conv != 0) return;
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr int NST = 3;
+  constexpr int RING = kWaveRing, PIN = kWavePin, nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
   constexpr int kConsumers = kThreads - 32;
+  constexpr int kStride = kWaveSlice * (4 + (int)sizeof(VT));   // bytes per entry column of a slice
+  static_assert((RING & (RING - 1)) == 0, "ring size must be a power of two");
+  static_assert(G == 1 || G == 2 || G == 4, "threads per row");
   // solution values: ring slots [0, RING), pinned long-range slots [RING, RING + PIN)
   VT* vals = reinterpret_cast<VT*>(smem);
   unsigned char* stage0 = smem + (RING + PIN) * sizeof(VT);
-  unsigned char* bstage0 = stage0 + NST * (size_t)stage_bytes;
-  __shared__ __align__(8) uint64_t full[NST];
-  __shared__ __align__(8) uint64_t empty[NST];
-  __shared__ WaveChunk sdesc[NST];
+  __shared__ __align__(8) uint64_t full[kWaveMaxStages];
+  __shared__ __align__(8) uint64_t empty[kWaveMaxStages];
+  __shared__ WaveChunk sdesc[kWaveMaxStages];
+  __shared__ int s_issued;   // copies the producer has started
+  __shared__ int s_abort;    // set by a consumer whose wait ran out (read after a barrier)
   const int tid = threadIdx.x;
   if (tid == 0) {
-    for (int s = 0; s < NST; s++) {
+    for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
+    s_issued = 0;
+    s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  volatile int* v_issued = &s_issued;
+  volatile int* v_abort = &s_abort;
 
   if (tid >= kConsumers) {
     // ---- producer ------------------------------------------------------------
-    if (tid == kConsumers) {
+    if (tid == kConsumers && nchunks > 0) {
+      WaveChunk next = chunks[0];
       for (int k = 0; k < nchunks; k++) {
-        const int s = k % NST;
-        if (k >= NST && !mbar_wait_bounded(&empty[s], (unsigned)(((k / NST) - 1) & 1))) {
+        const int s = k % nst;
+        const WaveChunk ch = next;
+        if (k + 1 < nchunks) next = chunks[k + 1];   // descriptor load overlaps the wait below
+        if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
           atomicOr(err, 8);
           break;
         }
-        const WaveChunk ch = chunks[k];
+        if (*v_abort) break;
         sdesc[s] = ch;
+        *v_issued = k + 1;
         fence_proxy_async();   // earlier generic reads of the stage precede the async refill
-        mbar_expect_tx(&full[s], (unsigned)(ch.img_bytes + ch.b_bytes));
+        mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
         bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s]);
-        bulk_g2s(bstage0 + s * (size_t)bstage_bytes, blev + ch.b_off, (unsigned)ch.b_bytes, &full[s]);
       }
     }
     return;
   }
 
   // ---- consumers -------------------------------------------------------------
-  const int g = tid & (kGroup - 1);
-  const int rows_per_pass = kConsumers / kGroup;
+  const int lane = tid & 31;
   for (int k = 0; k < nchunks; k++) {
-    const int s = k % NST;
-    if (!mbar_wait_bounded(&full[s], (unsigned)((k / NST) & 1))) {
-      if (tid == 0) atomicOr(err, 8);
-    }
-    const WaveChunk ch = sdesc[s];
-    const unsigned char* st = stage0 + s * (size_t)stage_bytes;
-    const int4* meta = reinterpret_cast<const int4*>(st);
-    const VT* diag = reinterpret_cast<const VT*>(st + ch.diag_off);
-    const VT* ev = reinterpret_cast<const VT*>(st + ch.val_off);
-    const int* es = reinterpret_cast<const int*>(st + ch.src_off);
-    const VT* bv = reinterpret_cast<const VT*>(bstage0 + s * (size_t)bstage_bytes);
-    const int m = ch.nrows;
-    for (int base = 0; base < m; base += rows_per_pass) {   // uniform trip count
-      const int r = base + tid / kGroup;
-      const bool valid = r < m;
+    const int s = k % nst;
+    const bool got = mbar_wait_bounded(&full[s], (unsigned)((k / nst) & 1));
+    if (!__all_sync(0xffffffffu, got)) {   // warp-uniform: the row sums below shuffle across lanes
+      atomicOr(err, 8);
+      *v_abort = 1;
+    } else {
+      const WaveChunk ch = sdesc[s];
+      const unsigned char* st = stage0 + s * (size_t)stage_bytes;
+      const int r = tid / G, g = tid & (G - 1);
+      const bool valid = r < ch.nrows;
+      int4 mt = make_int4(0, 0, 0, -1);   // row, entries, slice offset, pinned slot
       VT acc = 0;
-      int4 mt = make_int4(0, 0, 0, -1);
       if (valid) {
-        mt = meta[r];
-        for (int e = mt.y + g; e < mt.y + mt.z; e += kGroup) {
-          const int src = es[e];
-          const VT xv = (src >= 0) ? vals[src] : x[-src - 1];
-          acc += ev[e] * xv;
+        mt = reinterpret_cast<const int4*>(st)[r];
+        if (G == 1) acc = reinterpret_cast<const VT*>(st + ch.b_off)[r];
+        const unsigned char* col = st + mt.z;
+        const int* src = reinterpret_cast<const int*>(col) + lane;
+        const VT* val = reinterpret_cast<const VT*>(col + 4 * kWaveSlice) + lane;
+        constexpr int kS = kStride / 4;                 // column stride in int words
+        constexpr int kV = kStride / (int)sizeof(VT);   // column stride in values
+        const int cnt = mt.y > g ? (mt.y - g + G - 1) / G : 0;   // this lane's entries g, g+G, ...
+        int t = 0;
+        // batches of 8: all sources and values first, then the gathers, then the sums in order
+        for (; t + 8 <= cnt; t += 8) {
+          int sq[8];
+          VT vq[8], xq[8];
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            sq[q] = src[(t + q) * kS];
+            vq[q] = val[(t + q) * kV];
+          }
+#pragma unroll
+          for (int q = 0; q < 8; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
+#pragma unroll
+          for (int q = 0; q < 8; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
+        }
+        if (t + 4 <= cnt) {
+          int sq[4];
+          VT vq[4], xq[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            sq[q] = src[(t + q) * kS];
+            vq[q] = val[(t + q) * kV];
+          }
+#pragma unroll
+          for (int q = 0; q < 4; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
+          t += 4;
+        }
+        for (; t < cnt; t++) {
+          const int s0 = src[t * kS];
+          const VT v0 = val[t * kV];
+          const VT x0 = source_value<VT, FAR>(vals, x, s0);
+          acc = (LOWER || G > 1) ? fadd(acc, fmul(v0, x0)) : fadd(acc, -fmul(v0, x0));
         }
       }
-      acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-      acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+      if (G > 1) {
+        // G lanes per row: tree sum of the partial sums, then b +/- sum
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (valid) {
+          const VT b = reinterpret_cast<const VT*>(st + ch.b_off)[r];
+          acc = LOWER ? b + acc : b - acc;
+        }
+      }
       if (valid && g == 0) {
-        VT xi;
-        if (LOWER)
-          xi = bv[r] + acc;
-        else
-          xi = (bv[r] - acc) / diag[r];
-        vals[(ch.pos0 + r) % RING] = xi;
-        if (mt.w >= 0) vals[mt.w] = xi;
-        x[mt.x] = xi;
+        if (!LOWER) acc = acc / reinterpret_cast<const VT*>(st + ch.diag_off)[r];
+        vals[(ch.pos0 + r) & (RING - 1)] = acc;
+        if (mt.w >= 0) vals[mt.w] = acc;
+        x[mt.x] = acc;
       }
     }
     consumers_sync();                 // chunk k complete: its values are visible, its stage is free
+    if (*v_abort) {
+      // a copy never completed: stop, after giving the copies already started a bounded time to land
+      if (tid == 0)
+        for (int q = k; q < *v_issued; q++) mbar_wait_bounded(&full[q % nst], (unsigned)((q / nst) & 1), kDrainSpin);
+      return;
+    }
     if (tid == 0) mbar_arrive(&empty[s]);
   }
 }
 
-// right-hand side into padded level order
+// right-hand side into the chunk images (level order)
 template <class VT>
 __global__ void k_gather_lev(int n, const int* __restrict__ order, const int* __restrict__ bidx,
-                             const VT* __restrict__ b, VT* __restrict__ blev, const KrylovScalars* ks) {
+                             const VT* __restrict__ b, VT* __restrict__ img, const KrylovScalars* ks) {
   if (ks && ks->conv != 0) return;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) blev[bidx[p]] = b[order[p]];
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) img[bidx[p]] = b[order[p]];
 }
 
 // factor values into the chunk images (entries and, for U, the diagonal)
@@ -204,28 +281,34 @@ __global__ void k_pack_wave(int nent, const long long* __restrict__ ent_dst, con
 
 // ---- host side ----------------------------------------------------------------
 
+template <class VT, bool LOWER, int G, bool FAR>
+static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScalars* ks, size_t smem) {
+  static int attr_done = 0;
+  if (attr_done < (int)smem) {
+    cudaError_t e = cudaFuncSetAttribute(k_trsv_wave<VT, LOWER, G, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = (int)smem;
+  }
+  k_trsv_wave<VT, LOWER, G, FAR><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, x,
+                                                                      wd.stage_bytes, c->dev_err.p, ks);
+  return cudaGetLastError();
+}
+
 template <class VT, bool LOWER>
 static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, const KrylovScalars* ks) {
-  constexpr int RING = kWaveRing;
-  constexpr int PIN = kWavePin;
   const int n = c->neq;
   int nb = (n + 255) / 256;
   if (nb > c->num_sms * 4) nb = c->num_sms * 4;
-  VT* blev = reinterpret_cast<VT*>(wd.blev.p);
-  k_gather_lev<VT><<<nb, 256, 0, rg_counted(c)>>>(n, wd.order.p, wd.bidx.p, b, blev, ks);
-  const size_t smem = (RING + PIN) * sizeof(VT) + 3 * (size_t)wd.stage_bytes + 3 * (size_t)wd.bstage_bytes;
-  static bool attr_done[2][2] = {{false, false}, {false, false}};
-  bool& done = attr_done[sizeof(VT) == 8][LOWER];
-  cudaError_t e;
-  if (!done) {
-    e = cudaFuncSetAttribute(k_trsv_wave<VT, LOWER, RING, PIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    done = true;
-  }
-  k_trsv_wave<VT, LOWER, RING, PIN><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, blev, x,
-                                                             wd.stage_bytes, wd.bstage_bytes, c->dev_err.p, ks);
-  return cudaGetLastError();
+  k_gather_lev<VT><<<nb, 256, 0, rg_counted(c)>>>(n, wd.order.p, wd.bidx.p, b, reinterpret_cast<VT*>(wd.img.p), ks);
+  const int nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
+  const size_t smem = (kWaveRing + kWavePin) * sizeof(VT) + (size_t)nst * (size_t)wd.stage_bytes;
+  const bool far = wd.ring_misses > 0;
+  if (sizeof(VT) == 8 || wd.lanes == 1)
+    return far ? launch_wave_k<VT, LOWER, 1, true>(c, wd, x, ks, smem) : launch_wave_k<VT, LOWER, 1, false>(c, wd, x, ks, smem);
+  if (wd.lanes == 2)
+    return far ? launch_wave_k<VT, LOWER, 2, true>(c, wd, x, ks, smem) : launch_wave_k<VT, LOWER, 2, false>(c, wd, x, ks, smem);
+  return far ? launch_wave_k<VT, LOWER, 4, true>(c, wd, x, ks, smem) : launch_wave_k<VT, LOWER, 4, false>(c, wd, x, ks, smem);
 }
 
 cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void* y, const KrylovScalars* ks) {

@@ -6,17 +6,28 @@
 
 #include <algorithm>
 #include <cstring>
-
+#include <numeric>
 
 // Build the level-ordered chunk layout of one triangular factor.  `dep` lists,
-// per row, the rows it reads (L: columns < row, U: columns > row); `src_pos`
-// the factor positions of those entries; diag_pos the diagonal positions.
+// per row, the rows it reads (L: columns < row, U: columns > row) in the
+// factor's row order; `src_pos` the factor positions of those entries;
+// diag_pos the diagonal positions.
+//
+// Rows of one level do not depend on each other.  Inside a level they are
+// ordered by entry count, longest first, so that the rows of a warp slice
+// have similar lengths.  `lanes` threads share a row (a warp slice holds
+// 32 / lanes rows): lane g of a row takes its entries g, g + lanes, ...; with
+// one lane per row the entries are summed in the factor's order, which is the
+// order of PRECO_ILU0::Solve (Preco_ilu0.cpp:517-530, 964-980).
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
                              const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
-                             int vt_bytes, int ring, int pin, int stage_cap, int bstage_cap) {
+                             int vt_bytes, int ring, int pin, int stage_cap, int rows_max, int lanes) {
   WaveLayout w;
   w.n = n;
-  // dependency levels, rows of a level in solve order
+  const int rps = kWaveSlice / lanes;   // rows per warp slice
+  // all rows of a chunk write their ring slots at once: they must be distinct
+  rows_max = std::min(rows_max, ring);
+  // dependency levels
   std::vector<int> lev(n, 0);
   int nlev = 0;
   for (int t = 0; t < n; t++) {
@@ -30,49 +41,45 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   std::vector<int> cnt(nlev + 1, 0);
   for (int i = 0; i < n; i++) cnt[lev[i] + 1]++;
   for (int l = 0; l < nlev; l++) cnt[l + 1] += cnt[l];
+  // level order: by level, inside a level by entry count (descending), then solve order
   std::vector<int> order(n), pos(n), fill(cnt.begin(), cnt.end() - 1);
   for (int t = 0; t < n; t++) {
     const int i = lower ? t : n - 1 - t;
-    const int p = fill[lev[i]]++;
-    order[p] = i;
-    pos[i] = p;
+    order[fill[lev[i]]++] = i;
   }
+  auto kof = [&](int i) { return ptr[i + 1] - ptr[i]; };
+  for (int l = 0; l < nlev; l++)
+    std::stable_sort(order.begin() + cnt[l], order.begin() + cnt[l + 1],
+                     [&](int a, int b) { return kof(a) > kof(b); });
+  for (int p = 0; p < n; p++) pos[order[p]] = p;
+
   auto a16 = [](long long v) { return (v + 15) & ~15ll; };
-  // chunk image: meta[m] (int4) | diag[m] (VT) | vals[ne] (VT) | srcs[ne] (int), each part 16-aligned
-  auto img_size = [&](long long m, long long ne) {
-    return a16(16 * m) + a16(vt_bytes * m) + a16(vt_bytes * ne) + a16(4 * ne);
-  };
+  const long long stride = kWaveSlice * (4ll + vt_bytes);   // bytes per entry column of a slice
+  // chunk image: meta[m] (int4) | b[m] (VT) | diag[m] (VT, U only) | slices, each part 16-aligned
+  auto head_bytes = [&](long long m) { return a16(16 * m) + a16(vt_bytes * m) + (lower ? 0 : a16(vt_bytes * m)); };
   std::vector<int> chunk_end(n);
   int p = 0;
   long long img_off = 0;
-  int b_off = 0;
-  const int b_align = 16 / vt_bytes;
   while (p < n) {
     const int l = lev[order[p]];
     const int lend = cnt[l + 1];
     WaveChunk ch{};
     ch.pos0 = p;
-    int m = 0, ne = 0;
-    while (p + m < lend) {
-      const int i = order[p + m];
-      const int k = ptr[i + 1] - ptr[i];
-      if (m > 0 && (img_size(m + 1, ne + k) > stage_cap || a16((long long)vt_bytes * (m + 1)) > bstage_cap ||
-                    m + 1 > 4096))
-        break;
+    int m = 0;
+    long long ebytes = 0;
+    while (p + m < lend && m < rows_max) {
+      // a new slice starts every rps rows; its width is set by its first (longest) row
+      const long long add = (m % rps == 0) ? (long long)((kof(order[p + m]) + lanes - 1) / lanes) * stride : 0;
+      if (m > 0 && head_bytes(m + 1) + ebytes + add > stage_cap) break;
+      ebytes += add;
       m++;
-      ne += k;
     }
     ch.nrows = m;
-    ch.nent = ne;
-    ch.diag_off = (int)a16(16ll * m);
-    ch.val_off = (int)(ch.diag_off + a16((long long)vt_bytes * m));
-    ch.src_off = (int)(ch.val_off + a16((long long)vt_bytes * ne));
-    ch.img_bytes = (int)img_size(m, ne);
+    ch.b_off = (int)a16(16ll * m);
+    ch.diag_off = (int)(ch.b_off + a16((long long)vt_bytes * m));
+    ch.img_bytes = (int)(head_bytes(m) + ebytes);
     ch.img_off = img_off;
-    ch.b_off = b_off;
-    ch.b_bytes = (int)a16((long long)vt_bytes * m);
     img_off += ch.img_bytes;
-    b_off += ((m + b_align - 1) / b_align) * b_align;
     for (int r = 0; r < m; r++) chunk_end[p + r] = p + m;
     w.chunks.push_back(ch);
     p += m;
@@ -92,25 +99,31 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   for (size_t k = 0; k < cand.size() && (int)k < pin; k++) pin_slot[cand[k]] = (int)k;
   w.pinned = (int)std::min<size_t>(cand.size(), (size_t)pin);
   w.img_bytes = img_off;
-  w.blev_len = b_off + 16;
   w.order = order;
   w.bidx.resize(n);
   std::vector<unsigned char> img((size_t)img_off, 0);
   for (const WaveChunk& ch : w.chunks) {
-    int e = 0;
+    const int cend = ch.pos0 + ch.nrows;
+    long long sbase = head_bytes(ch.nrows);   // byte offset of the current slice in the chunk
+    int width = 0;
     for (int r = 0; r < ch.nrows; r++) {
       const int pp = ch.pos0 + r;
       const int i = order[pp];
-      w.bidx[pp] = ch.b_off + r;
-      const int k = ptr[i + 1] - ptr[i];
-      int mt[4] = {i, e, k, pin_slot[i] >= 0 ? ring + pin_slot[i] : -1};
+      const int rs = r % rps;   // row inside its slice
+      if (rs == 0) {
+        if (r > 0) sbase += (long long)width * stride;
+        width = (kof(i) + lanes - 1) / lanes;
+      }
+      w.bidx[pp] = (int)((ch.img_off + ch.b_off) / vt_bytes + r);
+      const int k = kof(i);
+      int mt[4] = {i, k, (int)sbase, pin_slot[i] >= 0 ? ring + pin_slot[i] : -1};
       std::memcpy(&img[(size_t)ch.img_off + 16 * (size_t)r], mt, 16);
       if (!lower) {
         w.diag_dst.push_back(ch.img_off + ch.diag_off + (long long)vt_bytes * r);
         w.diag_src.push_back(diag_pos[i]);
       }
-      const int cend = ch.pos0 + ch.nrows;
-      for (int q = ptr[i]; q < ptr[i + 1]; q++, e++) {
+      for (int e = 0; e < k; e++) {
+        const int q = ptr[i] + e;
         const int j = dep[q];
         const int pj = pos[j];
         int src;
@@ -120,8 +133,10 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
           src = ring + pin_slot[j];
         else
           src = -(j + 1);
-        std::memcpy(&img[(size_t)(ch.img_off + ch.src_off) + 4 * (size_t)e], &src, 4);
-        w.ent_dst.push_back(ch.img_off + ch.val_off + (long long)vt_bytes * e);
+        const int lane = rs * lanes + e % lanes;
+        const long long col = ch.img_off + sbase + (long long)(e / lanes) * stride;
+        std::memcpy(&img[(size_t)(col + 4ll * lane)], &src, 4);
+        w.ent_dst.push_back(col + 4ll * kWaveSlice + (long long)vt_bytes * lane);
         w.ent_src.push_back(src_pos[q]);
         if (src < 0) w.ring_misses++;
       }

@@ -27,7 +27,7 @@ static int fails = 0;
   } while (0)
 
 template <class VT>
-static void run(int n, int band, int seed, bool lower, int ring, int pin, int stage_cap, int bstage_cap) {
+static void run(int n, int band, int seed, bool lower, int ring, int pin, int stage_cap, int lanes) {
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> U(-1.0, 1.0);
   // random triangular structure within a band
@@ -54,7 +54,9 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
     val.push_back(1.5 + U(rng) * 0.2);
   }
   const int vtb = sizeof(VT);
-  WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, pin, stage_cap, bstage_cap);
+  const int rows_max = kWaveRows / lanes;
+  const int rps = 32 / lanes;
+  WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, pin, stage_cap, rows_max, lanes);
   // pack values as the device kernel does
   std::vector<unsigned char> img = w.img_host;
   for (size_t q = 0; q < w.ent_dst.size(); q++) {
@@ -67,49 +69,67 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
   }
   std::vector<VT> b(n);
   for (auto& v : b) v = (VT)U(rng);
-  std::vector<VT> blev(w.blev_len + 16, (VT)0);
-  for (int p = 0; p < n; p++) blev[w.bidx[p]] = b[w.order[p]];
-  // reference solve
+  // right-hand side into the images (k_gather_lev)
+  for (int p = 0; p < n; p++) {
+    CHECK((long long)w.bidx[p] * vtb + vtb <= (long long)img.size(), "rhs slot out of range");
+    std::memcpy(&img[(size_t)w.bidx[p] * vtb], &b[w.order[p]], sizeof(VT));
+  }
+  // reference solve, the summation order of PRECO_ILU0::Solve
   std::vector<VT> xr(n);
   for (int t = 0; t < n; t++) {
     int i = lower ? t : n - 1 - t;
-    VT acc = 0;
-    for (int q = ptr[i]; q < ptr[i + 1]; q++) acc += (VT)val[srcpos[q]] * xr[dep[q]];
-    xr[i] = lower ? b[i] + acc : (b[i] - acc) / (VT)val[diag_pos[i]];
+    VT acc = b[i];
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) {
+      VT prod = (VT)val[srcpos[q]] * xr[dep[q]];
+      acc = lower ? acc + prod : acc - prod;
+    }
+    xr[i] = lower ? acc : acc / (VT)val[diag_pos[i]];
   }
+  const long long stride = 32ll * (4 + vtb);
   for (int pass = 0; pass < 2; pass++) {
     std::vector<VT> ringv(ring + pin, (VT)NAN), x(n, (VT)NAN);
     int written = 0;
     for (const WaveChunk& ch : w.chunks) {
       CHECK(ch.img_off % 16 == 0 && ch.img_bytes % 16 == 0, "image alignment");
-      CHECK(ch.diag_off % 16 == 0 && ch.val_off % 16 == 0 && ch.src_off % 16 == 0, "part alignment");
+      CHECK(ch.b_off % 16 == 0 && ch.diag_off % 16 == 0, "part alignment");
       CHECK(ch.img_bytes <= stage_cap || ch.nrows == 1, "stage capacity %d > %d", ch.img_bytes, stage_cap);
-      CHECK((ch.b_off * vtb) % 16 == 0 && ch.b_bytes % 16 == 0, "rhs alignment");
-      CHECK(ch.b_bytes <= bstage_cap, "rhs stage capacity");
+      CHECK(ch.nrows >= 1 && ch.nrows <= rows_max, "rows per chunk");
       CHECK(ch.pos0 == written, "chunk positions contiguous");
       const unsigned char* st = &img[ch.img_off];
       for (int rr = 0; rr < ch.nrows; rr++) {
         int r = pass == 0 ? rr : ch.nrows - 1 - rr;
         int meta[4];
         std::memcpy(meta, st + 16 * r, 16);
-        VT acc = 0;
-        for (int e = meta[1]; e < meta[1] + meta[2]; e++) {
+        CHECK(meta[2] % 16 == 0 && meta[2] >= ch.diag_off, "slice offset");
+        CHECK(meta[2] + (long long)((meta[1] + lanes - 1) / lanes) * stride <= ch.img_bytes,
+              "slice inside the chunk image");
+        VT b_r;
+        std::memcpy(&b_r, st + ch.b_off + (size_t)vtb * r, sizeof(VT));
+        // lane g of the row sums entries g, g + lanes, ...; one lane: from b in the factor's order
+        VT part[4] = {0, 0, 0, 0};
+        if (lanes == 1) part[0] = b_r;
+        for (int e = 0; e < meta[1]; e++) {
+          const int g = e % lanes, lane = (r % rps) * lanes + g;
           VT v;
           int src;
-          std::memcpy(&v, st + ch.val_off + (size_t)vtb * e, sizeof(VT));
-          std::memcpy(&src, st + ch.src_off + (size_t)4 * e, 4);
+          std::memcpy(&src, st + meta[2] + (e / lanes) * stride + 4 * lane, 4);
+          std::memcpy(&v, st + meta[2] + (e / lanes) * stride + 128 + (size_t)vtb * lane, sizeof(VT));
           CHECK(src < ring + pin, "source slot out of range");
           VT xv = src >= 0 ? ringv[src] : x[-src - 1];
-          acc += v * xv;
+          VT prod = v * xv;
+          part[g] = (lower || lanes > 1) ? part[g] + prod : part[g] - prod;
         }
-        VT bv = blev[ch.b_off + r];
+        VT acc = part[0];
+        if (lanes == 2) acc = part[0] + part[1];
+        if (lanes == 4) acc = (part[0] + part[1]) + (part[2] + part[3]);
+        if (lanes > 1) acc = lower ? b_r + acc : b_r - acc;
         VT xi;
         if (lower) {
-          xi = bv + acc;
+          xi = acc;
         } else {
           VT d;
           std::memcpy(&d, st + ch.diag_off + (size_t)vtb * r, sizeof(VT));
-          xi = (bv - acc) / d;
+          xi = acc / d;
         }
         ringv[(ch.pos0 + r) % ring] = xi;
         if (meta[3] >= 0) {
@@ -121,27 +141,34 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
       written += ch.nrows;
     }
     CHECK(written == n, "all rows solved");
+    int bad = 0;
     double err = 0, scale = 1e-30;
     for (int i = 0; i < n; i++) {
+      bad += !(x[i] == xr[i]);
       err = std::max(err, (double)std::fabs(x[i] - xr[i]));
       scale = std::max(scale, (double)std::fabs(xr[i]));
     }
-    // same products, possibly different summation order: a few ulps
-    CHECK(err <= (vtb == 8 ? 1e-12 : 1e-4) * scale, "n=%d band=%d lower=%d pass=%d err=%g", n, band, (int)lower,
-          pass, err / scale);
+    if (lanes == 1)   // same products in the same order: identical results
+      CHECK(bad == 0, "n=%d band=%d lower=%d pass=%d: %d rows differ", n, band, (int)lower, pass, bad);
+    else              // split sums: a few ulps
+      CHECK(err <= 1e-4 * scale, "n=%d band=%d lower=%d pass=%d lanes=%d err=%g", n, band, (int)lower, pass, lanes,
+            err / scale);
   }
 }
 
 int main() {
+  const int st32 = 49408, st64 = 33280;   // the stage sizes of the library's shared-memory budget
   for (int lower = 0; lower < 2; lower++) {
     for (int n : {1, 2, 7, 64, 1000, 20000}) {
       for (int band : {1, 3, 50, 600}) {
-        run<double>(n, band, n + band, lower, kWaveRing, kWavePin, kWaveStage64, kWaveBStage64);
-        run<float>(n, band, n + band + 1, lower, kWaveRing, kWavePin, kWaveStage32, kWaveBStage32);
+        run<double>(n, band, n + band, lower, kWaveRing, kWavePin, st64, kWaveLanes64);
+        run<float>(n, band, n + band + 1, lower, kWaveRing, kWavePin, st32, kWaveLanes32);
+        run<float>(n, band, n + band + 5, lower, kWaveRing, kWavePin, st32, 1);
+        run<double>(n, band, n + band + 6, lower, kWaveRing, kWavePin, st64, 2);
         // tiny rings, pinned tables and stages force pinning, global reads and level splitting
-        run<double>(n, band, n + band + 2, lower, 64, 16, 1024, 64);
-        run<float>(n, band, n + band + 3, lower, 32, 0, 512, 32);
-        run<float>(n, band, n + band + 4, lower, 16, 4096, 512, 32);
+        run<double>(n, band, n + band + 2, lower, 64, 16, 4096, 1);
+        run<float>(n, band, n + band + 3, lower, 32, 0, 2048, 4);
+        run<float>(n, band, n + band + 4, lower, 16, 4096, 2048, 4);
       }
     }
   }
