@@ -51,7 +51,7 @@ FP64_KRYLOV_PER_STEP = 861.5
 # DRAM bytes (read + write) of one k_trsv_wave<float, LOWER> launch on this
 # workload, from the ncu capture summarised in
 # profiles/k_trsv_wave_meander200k.txt (cold L2, kernel replay)
-NCU_TRSV_TRAFFIC_BYTES = 13.737984e6
+NCU_TRSV_TRAFFIC_BYTES = 14.733312e6
 
 
 def workload():

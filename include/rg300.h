@@ -189,7 +189,8 @@ rg_status rg_friction(rg_ctx* ctx, double* cf_out);
 
 /* Device-time of the last call's kernels, by stage (ms), for measurement:
  * [0] assembly, [1] scale, [2] factor, [3] BiCGStab total, [4] SpMV (one),
- * [5] ILU apply (one), [6] update, [7] friction. */
+ * [5] ILU apply (one), [6] update, [7] friction; [8] / [9] host time of the
+ * last / of all rg_set_pattern calls (schedules and layouts are built there). */
 rg_status rg_get_timings(rg_ctx* ctx, double* ms, int n);
 
 /* Structure of the resident system: [0] neq, [1] nnz, [2] dependency depth of

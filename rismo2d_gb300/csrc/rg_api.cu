@@ -5,6 +5,7 @@
 #include "rg_internal.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -373,7 +374,7 @@ rg_status rg_destroy(rg_ctx* c) {
   return RG_OK;
 }
 
-rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index, const int* eqno) {
+static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const int* index, const int* eqno) {
   if (!c || neq <= 0 || !width || !index || !eqno) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: bad arguments");
   TRY(cudaSetDevice(c->device));
   // CRS layout
@@ -617,6 +618,17 @@ rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index,
   c->have_factor = false;
   TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
+}
+
+rg_status rg_set_pattern(rg_ctx* c, int neq, const int* width, const int* index, const int* eqno) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const rg_status st = set_pattern_impl(c, neq, width, index, eqno);
+  if (c) {
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    c->t_ms[8] = ms;
+    c->t_ms[9] += ms;
+  }
+  return st;
 }
 
 rg_status rg_set_boundary(rg_ctx* c, const int* nflag, const int* bckind, const double* rot, const double* niox,
@@ -1069,7 +1081,7 @@ rg_status rg_event_elapsed(rg_ctx* c, int a, int b, double* ms) {
 
 rg_status rg_get_timings(rg_ctx* c, double* ms, int n) {
   if (!c || !ms) return RG_ERR_ARG;
-  for (int i = 0; i < n && i < 8; i++) ms[i] = c->t_ms[i];
+  for (int i = 0; i < n && i < 10; i++) ms[i] = c->t_ms[i];
   return RG_OK;
 }
 

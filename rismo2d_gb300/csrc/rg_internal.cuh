@@ -188,7 +188,7 @@ struct rg_ctx {
 
   // timings
   cudaEvent_t ev[16];
-  double t_ms[8] = {0};
+  double t_ms[10] = {0};   // device ms by stage; [8] / [9] host ms of the last / all rg_set_pattern calls
 
   int persist_blocks = 0;    // co-resident blocks for the persistent kernels
   WaveDev waveL, waveU;      // wavefront triangular solves
