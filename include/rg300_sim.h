@@ -97,6 +97,8 @@ typedef struct {
   double residual_ratio;       /* last ||B_k|| / ||B_0|| */
   double wall_ms;
   double residual_hist[64];
+  int    warm_start;           /* 1: the step started from the state given to rg_sim_set_warm_start */
+  double residual_warm;        /* ||B|| at that state (-1: none given) */
 } rg_step_report;
 
 /* device >= 0: GPU ordinal; RG_DEVICE_NONE: host model only (numbering and
@@ -111,6 +113,15 @@ rg_status rg_sim_set_state(rg_sim* sim, const double* U, const double* V, const 
 rg_status rg_sim_get_state(rg_sim* sim, double* U, double* V, double* S, double* z, int* nflag);
 /* one time step [t, t+dt] (EQS_UVS2D::Execute + Compute.cpp:774-810) */
 rg_status rg_sim_step(rg_sim* sim, double t, double dt, const rg_step_ctl* ctl, rg_step_report* rep);
+/* Starting state of the next rg_sim_step's Newton iteration (e.g. the learned
+ * prediction of include/rg300_mlp.h), used once: after the step's first
+ * dry/rewet pass it replaces U, V, S on the wet nodes (mid-side S as corner
+ * means, depth at least half the dry limit), and is kept only if its residual
+ * ||B|| is below that of the last time level; the step's ||B_0|| stays the
+ * last time level's, so the convergence target is unchanged.  NULL arrays
+ * cancel a pending start.  No counterpart in the reference
+ * (EQS_UVS2D::Predict, EqsUVS2D.cpp:1101, starts from the last time level). */
+rg_status rg_sim_set_warm_start(rg_sim* sim, const double* U, const double* V, const double* S);
 /* the host part of one Newton iteration's set-up with the given nodal
  * friction (InitBcon at time t_bc, SetLocation, SetNormal, SetRotation,
  * SetEqno when the model changed) -- no GPU work */

@@ -36,7 +36,11 @@ EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pat
            "rg_sim_get_boundary", "rg_set_elements", "rg_set_old", "rg_get_dt", "rg_timegrad",
            "rg_zero_velocity", "rg_sim_dry_rewet", "rg_get_stats", "rg_event_record", "rg_event_elapsed",
            "rg_sim_context", "rg_profile", "rg_profile_read", "rg_sim_get_model",
-           "rg_ilu0_apply_dev_noalloc"]
+           "rg_ilu0_apply_dev_noalloc",
+           "rg_mlp_create", "rg_mlp_destroy", "rg_mlp_last_error", "rg_mlp_set_mesh", "rg_mlp_set_scales",
+           "rg_mlp_get_params", "rg_mlp_set_params", "rg_mlp_features", "rg_mlp_add_samples",
+           "rg_mlp_clear_samples", "rg_mlp_train", "rg_mlp_loss_grad", "rg_mlp_predict",
+           "rg_sim_set_warm_start"]
 
 
 class RgMesh(C.Structure):

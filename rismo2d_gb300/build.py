@@ -16,8 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librg300.so")
-SOURCES = ["rg_assemble.cu", "rg_linalg.cu", "rg_trsv.cu", "rg_api.cu", "rg_noalloc.cu", "rg_model.cpp",
-           "rg_wave_layout.cpp"]
+SOURCES = ["rg_assemble.cu", "rg_linalg.cu", "rg_trsv.cu", "rg_api.cu", "rg_noalloc.cu", "rg_mlp.cu",
+           "rg_model.cpp", "rg_wave_layout.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -32,7 +32,8 @@ def _nvcc() -> str:
 def _compile(src: str) -> str:
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     deps = [os.path.join(CSRC, src), os.path.join(CSRC, "rg_internal.cuh"),
-            os.path.join(HERE, "..", "include", "rg300.h"), os.path.join(HERE, "..", "include", "rg300_sim.h")]
+            os.path.join(HERE, "..", "include", "rg300.h"), os.path.join(HERE, "..", "include", "rg300_sim.h"),
+            os.path.join(HERE, "..", "include", "rg300_mlp.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     if src.endswith(".cpp"):

@@ -134,6 +134,9 @@ struct rg_sim {
   bool have_state = false;
   // last step report detail
   std::vector<double> resid_hist;
+  // warm start of the next step (rg_sim_set_warm_start)
+  bool warm_pending = false;
+  std::vector<double> wU, wV, wS;
 };
 
 static rg_status sfail(rg_sim* s, rg_status st, const std::string& m) {
@@ -985,6 +988,19 @@ rg_status rg_sim_get_model(rg_sim* s, int* ne, int* elem_nodes, int* elem_nnd, i
   return RG_OK;
 }
 
+rg_status rg_sim_set_warm_start(rg_sim* s, const double* U, const double* V, const double* S) {
+  if (!s || !s->have_state) return RG_ERR_ARG;
+  if (!U || !V || !S) {
+    s->warm_pending = false;
+    return RG_OK;
+  }
+  s->wU.assign(U, U + s->np);
+  s->wV.assign(V, V + s->np);
+  s->wS.assign(S, S + s->np);
+  s->warm_pending = true;
+  return RG_OK;
+}
+
 rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg_step_report* rep) {
   if (!s || !ctl || !s->have_state || dt <= 0.0) return RG_ERR_ARG;
   if (!s->ctx) return sfail(s, RG_ERR_ARG, "rg_sim_step: created without a GPU context");
@@ -1019,6 +1035,8 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
   int nextDW = 0;
   int maxit = ctl->max_newton > 0 ? ctl->max_newton : s->p.max_newton;
   double first_norm = -1.0;
+  double warm_res = -1.0;
+  int warm_used = 0;
   int krylov_total = 0, newton = 0, dw_events = 0;
   bool converged = false;
   bool state_on_device = false;
@@ -1068,49 +1086,89 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       if (st != RG_OK) return st;
       state_on_device = true;
     }
-    // friction (GPU) and boundary data (host) of this iteration
-    STAGE("friction");
-    st = rg_friction(s->ctx, s->cf.data());
-    if (st != RG_OK) return st;
-    if (!s->bcl.empty()) {
-      // the inlet distribution reads S, z at the inlet nodes: the device copy is current
-      st = rg_get_state(s->ctx, nullptr, nullptr, s->S.data(), s->z.data());
+    // friction (GPU), boundary data (host), assembly and scaling of the current state: ||B|| is the
+    // Newton residual
+    auto build_system = [&](double* scale) -> rg_status {
+      rg_status st;
+      // friction (GPU) and boundary data (host) of this iteration
+      STAGE("friction");
+      st = rg_friction(s->ctx, s->cf.data());
       if (st != RG_OK) return st;
-    }
-    STAGE("init_bcon");
-    if (init_bcon(s, t + dt)) {
-      st = rg_set_state(s->ctx, nullptr, nullptr, s->S.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
-                        nullptr);
+      if (!s->bcl.empty()) {
+        // the inlet distribution reads S, z at the inlet nodes: the device copy is current
+        st = rg_get_state(s->ctx, nullptr, nullptr, s->S.data(), s->z.data());
+        if (st != RG_OK) return st;
+      }
+      STAGE("init_bcon");
+      if (init_bcon(s, t + dt)) {
+        st = rg_set_state(s->ctx, nullptr, nullptr, s->S.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                          nullptr);
+        if (st != RG_OK) return st;
+      }
+      set_location(s);
+      set_normal(s);
+      std::vector<int> zero_uv;
+      set_rotation(s, &zero_uv);
+      if (!zero_uv.empty()) {
+        st = rg_zero_velocity(s->ctx, (int)zero_uv.size(), zero_uv.data());
+        if (st != RG_OK) return st;
+      }
+      if (s->eqs_init != s->model_init) {
+        s->eqs_init = s->model_init;
+        STAGE("set_eqno");
+        st = set_eqno(s);
+        if (st != RG_OK) return st;
+        STAGE("push_model");
+        st = push_model(s);
+        if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
+        st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
+        if (st != RG_OK) return st;
+      }
+      st = push_boundary(s);
       if (st != RG_OK) return st;
-    }
-    set_location(s);
-    set_normal(s);
-    std::vector<int> zero_uv;
-    set_rotation(s, &zero_uv);
-    if (!zero_uv.empty()) {
-      st = rg_zero_velocity(s->ctx, (int)zero_uv.size(), zero_uv.data());
+      // assemble, scale: ||B_k|| is the Newton residual
+      STAGE("assemble");
+      st = rg_assemble(s->ctx, nullptr, nullptr, nullptr);
       if (st != RG_OK) return st;
-    }
-    if (s->eqs_init != s->model_init) {
-      s->eqs_init = s->model_init;
-      STAGE("set_eqno");
-      st = set_eqno(s);
-      if (st != RG_OK) return st;
-      STAGE("push_model");
-      st = push_model(s);
-      if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
-      st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
-      if (st != RG_OK) return st;
-    }
-    st = push_boundary(s);
-    if (st != RG_OK) return st;
-    // assemble, scale: ||B_k|| is the Newton residual
-    STAGE("assemble");
-    st = rg_assemble(s->ctx, nullptr, nullptr, nullptr);
-    if (st != RG_OK) return st;
+      return rg_scale(s->ctx, scale);
+    };
     double scale = 0.0;
-    st = rg_scale(s->ctx, &scale);
+    st = build_system(&scale);
     if (st != RG_OK) return st;
+    if (it == 0 && s->warm_pending) {
+      // learned warm start: the predicted state replaces the last time level on the
+      // wet nodes if its residual is the smaller one; ||B_0|| stays the plain start's
+      s->warm_pending = false;
+      const std::vector<double> pU = s->U, pV = s->V, pS = s->S;
+      for (int n : s->mnodes) {
+        s->U[n] = s->wU[n];
+        s->V[n] = s->wV[n];
+        s->S[n] = std::max(s->wS[n], s->z[n] + 0.5 * s->p.dry_limit);
+      }
+      for (int e = 0; e < s->ne; e++) {   // mid-side S as the corner mean (k_upd_midside)
+        if (s->eflag[e] & E_DRY) continue;
+        const int* nd = &s->en[6 * e];
+        for (int k = 0; k < 3; k++) s->S[nd[3 + k]] = 0.5 * (s->S[nd[k]] + s->S[nd[(k + 1) % 3]]);
+      }
+      st = push_state(s);
+      if (st == RG_OK && !steady) st = rg_timegrad(s->ctx, dt, th);
+      double wscale = 0.0;
+      if (st == RG_OK) st = build_system(&wscale);
+      if (st != RG_OK) return st;
+      warm_res = wscale;
+      if (wscale < scale) {
+        warm_used = 1;
+        first_norm = scale;
+        scale = wscale;
+      } else {
+        s->U = pU;
+        s->V = pV;
+        s->S = pS;
+        st = push_state(s);   // host time derivatives are still the predictor's zeros
+        if (st == RG_OK) st = build_system(&scale);
+        if (st != RG_OK) return st;
+      }
+    }
     if (first_norm < 0.0) first_norm = scale;
     s->resid_hist.push_back(scale);
     last_ratio = first_norm > 0.0 ? scale / first_norm : 0.0;
@@ -1196,6 +1254,8 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       if (s->nflag[n] & N_DRY) nd++;
     rep->dry_nodes = nd;
     rep->solver_status = status_solve;
+    rep->warm_start = warm_used;
+    rep->residual_warm = warm_res;
   }
   return converged ? RG_OK : RG_NOT_CONVERGED;
 }

@@ -50,7 +50,8 @@ class StepReport(C.Structure):
     _fields_ = [("newton_iterations", C.c_int), ("krylov_iterations", C.c_int), ("converged", C.c_int),
                 ("neq", C.c_int), ("dryrew_events", C.c_int), ("dry_nodes", C.c_int), ("solver_status", C.c_int),
                 ("n_hist", C.c_int), ("residual_first", C.c_double), ("residual_ratio", C.c_double),
-                ("wall_ms", C.c_double), ("residual_hist", C.c_double * 64)]
+                ("wall_ms", C.c_double), ("residual_hist", C.c_double * 64), ("warm_start", C.c_int),
+                ("residual_warm", C.c_double)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "residual_hist"}
@@ -162,6 +163,13 @@ class Simulation:
         if st != _lib.RG_OK:
             raise _lib.RgError(st, "rg_sim_set_state: " + self._err())
         self.step_no = 0
+
+    def set_warm_start(self, U, V, S):
+        """Starting state of the next step's Newton iteration (kept only if its residual is smaller)."""
+        U, V, S = (np.ascontiguousarray(v, np.float64) for v in (U, V, S))
+        st = self.lib.rg_sim_set_warm_start(self.ptr, p(U), p(V), p(S))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_set_warm_start: " + self._err())
 
     def get_state(self) -> dict:
         out = {k: np.zeros(self.np) for k in ("U", "V", "S", "z")}

@@ -11,7 +11,7 @@ REPO = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 
 def header_functions():
     names = set()
-    for h in ("rg300.h", "rg300_sim.h"):
+    for h in ("rg300.h", "rg300_sim.h", "rg300_mlp.h"):
         text = open(os.path.join(REPO, "include", h)).read()
         names |= set(re.findall(r"^\s*(?:rg_status|const char\*|rg_ctx\*)\s+(rg_\w+)\s*\(", text, re.M))
     return sorted(names)
