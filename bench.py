@@ -10,12 +10,17 @@ Q(t) = 300 + 500 sin^2(pi t / 7200) m^3/s, outlet level fixed, dry/rewet
 method 2 every 10 Newton iterations.  Every time step runs Newton until the
 scaled residual ||B_k|| / ||B_0|| <= 1e-8.
 
-A "step" is one such time step.  Default arm: the mixed-precision solver
-(FP32 Krylov / SpMV / ILU(0) inside FP64 iterative refinement, FP64 residual
-and update) is the headline; the plain FP64 GPU path runs the same time steps
-for comparison; the CPU restatement of the reference's solver is timed on a
-bounded sample on the host cores.  `--impl reference` times that CPU solver
-alone.  One JSON line on stdout.
+A "step" is one such time step.  Default arm (the headline): the
+mixed-precision solver (FP32 Krylov / SpMV / ILU(0) inside FP64 iterative
+refinement, FP64 residual and update) started from the learned warm start.
+The network is trained on the GPU, before the timed region, on a trajectory
+of the plain mixed solver under a different hydrograph (Q(t) = 250 + 700
+sin^2(pi t / 5400), 12 steps from rest); the timed steps are held out.  Each
+timed step includes the prediction (features + forward pass, host copies in
+and out).  The same time steps also run cold-started (mixed, no warm start)
+and with the plain FP64 GPU path for comparison; the CPU restatement of the
+reference's solver is timed on a bounded sample on the host cores.
+`--impl reference` times that CPU solver alone.  One JSON line on stdout.
 """
 
 from __future__ import annotations
@@ -38,6 +43,11 @@ RESIDUAL_TOL = 1.0e-8
 METRIC = "s per time step at 1e-8 Newton residual: mixed+learned vs plain FP64, 1 GB300"
 WORKLOAD = ("meander 10 km x 601 m, 200,028 P2 triangles (402,747 nodes), unsteady dt=10 s, "
             "Q(t)=300+500 sin^2(pi t/7200), dry/rewet on, Newton to ||B||/||B0||<=1e-8")
+# training trajectory of the warm-start network: another hydrograph, from rest
+TRAIN_HYDROGRAPH = dict(Q0=250.0, dQ=700.0, period=5400.0, t_end=7200.0)
+TRAIN_STEPS = 12
+TRAIN_EPOCHS = 30
+TRAIN_BATCH = 8192
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
@@ -157,25 +167,72 @@ def l2_flush(buf):
     torch.cuda.synchronize()
 
 
+def train_net(device: int, max_newton: int = 0):
+    """The warm-start network of the workload's mesh, trained on the GPU on the plain mixed
+    solver's trajectory under the training hydrograph (not the timed one)."""
+    from rismo2d_gb300 import _lib, meshgen
+    from rismo2d_gb300 import warmstart as ws
+    from rismo2d_gb300.sim import Simulation, RG_CRIT_RESIDUAL
+    mesh, _hyd, params = workload()
+    hyd = meshgen.sin2_hydrograph(**TRAIN_HYDROGRAPH)
+    t0 = time.perf_counter()
+    sim = Simulation(mesh, params, hydrograph=hyd, precision=_lib.PREC_MIXED, device=device)
+    sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+    states, times, reps = ws.collect_trajectory(sim, hyd, 0.0, STEP_DT, TRAIN_STEPS, criterion=RG_CRIT_RESIDUAL,
+                                                residual_tol=RESIDUAL_TOL, max_newton=max_newton)
+    sim.close()
+    t1 = time.perf_counter()
+    net = ws.WarmStartNet(mesh, device=device, seed=7)
+    net.set_scales((4.0, 1.0, 1.0), *ws.trajectory_scales(states))
+    nsamp = ws.add_trajectory(net, states, times, hyd, STEP_DT)
+    losses = net.train(epochs=TRAIN_EPOCHS, batch=TRAIN_BATCH, lr=1e-3, seed=3)
+    t2 = time.perf_counter()
+    info = {"hydrograph": "Q(t)=250+700 sin^2(pi t/5400) from rest (held out from the timed steps)",
+            "trajectory_steps": TRAIN_STEPS, "samples": int(nsamp), "epochs": TRAIN_EPOCHS, "batch": TRAIN_BATCH,
+            "loss_first_last": [round(float(losses[0]), 4), round(float(losses[-1]), 4)],
+            "trajectory_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2),
+            "converged": all(r["converged"] for r in reps)}
+    return net, info
+
+
 def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, clocks: Clocks | None, dist: Dist,
-            flush_buf, max_newton: int = 0):
+            flush_buf, max_newton: int = 0, net=None):
     """W warm-up and K timed time steps through Simulation.step; per-step device time by
-    CUDA events on the library's stream, host wall time of step + state download."""
+    CUDA events on the library's stream, host wall time of step + state download.  With
+    `net`, every step after the first starts from the network's prediction; the
+    prediction's wall time (its kernels on the network's stream, copies in and out)
+    is added to the step's device time."""
     import torch
+    from rismo2d_gb300 import warmstart as ws
     from rismo2d_gb300.sim import Simulation, RG_CRIT_RESIDUAL
     mesh, hyd, params = workload()
     sim = Simulation(mesh, params, hydrograph=hyd, precision=prec, device=device)
     sim.set_state(mesh.U0, mesh.V0, mesh.S0)
     t = 0.0
     reps = []
+    hist = [sim.get_state()] if net else []
+
+    def predict():
+        if net is None or len(hist) < 2:
+            return 0.0, 0, 0
+        p0 = time.perf_counter()
+        sim.set_warm_start(*ws.predict_next(net, hist[-2], hist[-1], t, hyd, STEP_DT))
+        nwet = int(np.count_nonzero(ws.wet(hist[-1])))
+        # network copies: 6 state arrays + node list in, 4 floats per wet node out
+        return (time.perf_counter() - p0) * 1e3, 6 * 8 * mesh.np + 4 * nwet, 16 * nwet
+
     for _ in range(warmup):
+        predict()
         reps.append(sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL,
                              max_newton=max_newton))
         t += STEP_DT
+        if net:
+            hist = [hist[-1], sim.get_state()]
     st0 = sim.stats()
     if profile:
         sim.profile(True, reset=True)
     dev_ms, e2e_ms, timed = [], [], []
+    pred_h2d = pred_d2h = 0
     states = []
     dist.barrier()
     torch.cuda.synchronize()
@@ -185,12 +242,17 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
     for _ in range(steps):
         l2_flush(flush_buf)
         h0 = time.perf_counter()
+        pred_ms, bi, bo = predict()
+        pred_h2d += bi
+        pred_d2h += bo
         sim.event_record(0)
         rep = sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL, max_newton=max_newton)
         sim.event_record(1)
         state = sim.get_state()               # result to host memory (numpy)
         h1 = time.perf_counter()
-        dev_ms.append(sim.event_elapsed(0, 1))
+        if net:
+            hist = [hist[-1], state]
+        dev_ms.append(sim.event_elapsed(0, 1) + pred_ms)
         e2e_ms.append((h1 - h0) * 1e3)
         timed.append(rep)
         states.append({k: state[k] for k in ("U", "V", "S", "flag")})
@@ -203,9 +265,10 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
     prof = sim.profile_read() if profile else None
     if profile:
         sim.profile(False)
+    # the network's launches per prediction: features + forward
     out = dict(dev_ms=dev_ms, e2e_ms=e2e_ms, wall_s=wall1 - wall0, reps=timed, warm_reps=reps, states=states,
-               stats=st1.tolist(), h2d=int(st1[12] - st0[12]), d2h=int(st1[13] - st0[13]),
-               launches=int(st1[14] - st0[14]), prof=prof, clocks=clk)
+               stats=st1.tolist(), h2d=int(st1[12] - st0[12]) + pred_h2d, d2h=int(st1[13] - st0[13]) + pred_d2h,
+               launches=int(st1[14] - st0[14]) + (2 * steps if net else 0), prof=prof, clocks=clk)
     sim.close()
     return out
 
@@ -342,6 +405,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the plain FP64 comparison (0: skip)")
+    ap.add_argument("--cold-steps", type=int, default=5,
+                    help="timed steps of the mixed solver without warm start (0: skip)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU solver sampling (0: skip)")
     ap.add_argument("--max-newton", type=int, default=0,
                     help="cap on Newton iterations per step, for short profiling runs only (0: none; a capped "
@@ -381,7 +446,10 @@ def main():
     flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}")   # 256 MiB > L2
     from rismo2d_gb300 import _lib
     clocks = Clocks(device)
-    mixed = run_gpu(_lib.PREC_MIXED, warmup, args.steps, device, True, clocks, dist, flush_buf, args.max_newton)
+    net, learned_info = train_net(device, args.max_newton)
+    mixed = run_gpu(_lib.PREC_MIXED, warmup, args.steps, device, True, clocks, dist, flush_buf, args.max_newton,
+                    net=net)
+    net.close()
     k = args.steps
     dev_s = sum(mixed["dev_ms"]) / 1e3
     dev_s_max = dist.max(dev_s)
@@ -390,25 +458,40 @@ def main():
     newton = [r["newton_iterations"] for r in mixed["reps"]]
     krylov = [r["krylov_iterations"] for r in mixed["reps"]]
     conv = all(r["converged"] for r in mixed["reps"])
-    fp64 = None
-    if args.fp64_steps > 0:
-        kf = min(args.fp64_steps, k)
-        f = run_gpu(_lib.PREC_FP64, warmup, kf, device, False, None, dist, flush_buf, args.max_newton)
-        fs = sum(f["dev_ms"]) / 1e3 / kf
+
+    def rel_errs(sa, sb):
         errs = []
-        for j in range(kf):
-            a, b = mixed["states"][j], f["states"][j]
+        for a, b in zip(sa, sb):
             wet = (b["flag"] & 64) == 0               # NODE::kDry
             rel = {v: float(np.max(np.abs(a[v][wet] - b[v][wet])) / max(1e-30, np.max(np.abs(b[v][wet]))))
                    for v in ("U", "V", "S")}
             rel["flags_identical"] = bool(np.array_equal(a["flag"], b["flag"]))
             errs.append(rel)
+        return errs
+
+    cold = None
+    if args.cold_steps > 0:
+        kc = min(args.cold_steps, k)
+        c = run_gpu(_lib.PREC_MIXED, warmup, kc, device, False, None, dist, flush_buf, args.max_newton)
+        cs = sum(c["dev_ms"]) / 1e3 / kc
+        cold = {"s_per_step": round(cs, 4), "steps": kc,
+                "newton_per_step": statistics.mean(r["newton_iterations"] for r in c["reps"]),
+                "krylov_per_step": statistics.mean(r["krylov_iterations"] for r in c["reps"]),
+                "converged": all(r["converged"] for r in c["reps"]),
+                "learned_speedup": round(cs / (sum(mixed["dev_ms"][:kc]) / 1e3 / kc), 3),
+                "learned_vs_cold_max_rel_err": rel_errs(mixed["states"][:kc], c["states"])}
+    fp64 = None
+    if args.fp64_steps > 0:
+        kf = min(args.fp64_steps, k)
+        f = run_gpu(_lib.PREC_FP64, warmup, kf, device, False, None, dist, flush_buf, args.max_newton)
+        fs = sum(f["dev_ms"]) / 1e3 / kf
+        errs = rel_errs(mixed["states"][:kf], f["states"])
         fp64 = {"s_per_step": round(fs, 4), "steps": kf,
                 "newton_per_step": statistics.mean(r["newton_iterations"] for r in f["reps"]),
                 "krylov_per_step": statistics.mean(r["krylov_iterations"] for r in f["reps"]),
                 "converged": all(r["converged"] for r in f["reps"]),
-                "mixed_speedup": round(fs / (dev_s / k), 3),
-                "mixed_vs_fp64_max_rel_err": errs}
+                "learned_mixed_speedup": round(fs / (sum(mixed["dev_ms"][:kf]) / 1e3 / kf), 3),
+                "learned_mixed_vs_fp64_max_rel_err": errs}
     cpu = None
     if dist.rank == 0 and args.cpu_budget > 0:
         nps = fp64["newton_per_step"] if fp64 else statistics.mean(newton)
@@ -425,13 +508,15 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov/ILU(0) + f64 refinement",
                 "data": "synthetic (seeded meander mesh, no external dataset)",
                 "config": {"workload": WORKLOAD, "solver": "mixed: FP32 BiCGStab/ILU(0)/SpMV in FP64 iterative "
-                           "refinement; learned warm start not built", "precision_arm": "mixed",
+                           "refinement, started from the learned warm start (prediction inside each timed step)",
+                           "precision_arm": "mixed+learned",
                            "parallelism": "replicas only" if dist.world > 1 else "1 GPU",
                            "l2": "256 MiB buffer written between timed steps (the ~60 MB system stays "
                                  "L2-resident within a step)",
                            "neq": int(st[0]), "nnz": int(st[1])},
                 "newton_per_step": statistics.mean(newton), "krylov_per_step": statistics.mean(krylov),
-                "converged": conv, "fp64": fp64,
+                "converged": conv, "warm_start_accepted": sum(r["warm_start"] for r in mixed["reps"]),
+                "learned": learned_info, "cold_start": cold, "fp64": fp64,
                 "clocks": mixed["clocks"],
                 "e2e": {"value": round(e2e_s, 4), "unit": "s/step",
                         "h2d_bytes_per_step": mixed["h2d"] // k, "d2h_bytes_per_step": mixed["d2h"] // k,

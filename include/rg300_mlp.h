@@ -1,10 +1,12 @@
 /*
  * rg300 learned Newton warm start -- C ABI.
  *
- * A small per-node network predicts the change of U, V and S over the next
- * time step from the last two time levels on a one-ring mesh stencil, the bed
- * elevation and the inflow-discharge ratio.  The prediction is only a
- * starting point for the Newton iteration of rg_sim_step: the plain Newton /
+ * A small per-node network predicts U, V and S of the next time level from
+ * the last two time levels on a one-ring mesh stencil, the bed elevation and
+ * the inflow-discharge ratio: its outputs correct the linear extrapolation
+ * 2 L1 - L2 of the last two levels (L1 where the node was dry at level 2).
+ * The prediction is only a starting point for the Newton iteration of
+ * rg_sim_step: the plain Newton /
  * BiCGStab iteration still judges convergence, and the step starts from the
  * previous time level whenever the predicted start has the larger residual.
  * No counterpart in the reference (EQS_UVS2D::Predict, EqsUVS2D.cpp:1101,
@@ -50,9 +52,11 @@ const char* rg_mlp_last_error(rg_mlp* mlp);
 rg_status rg_mlp_set_mesh(rg_mlp* mlp, int np, const double* x, const double* y, const double* z,
                           int ne, const int* elem_nodes);
 
-/* Reference scales: inputs H [m], velocity [m/s], bed difference [m]; outputs
- * (the scale of one step's change of U, V, S). */
-rg_status rg_mlp_set_scales(rg_mlp* mlp, const float* in_ref3, const float* out_scale3);
+/* Scales: in_ref3 = inputs H [m], velocity [m/s], bed difference [m];
+ * step_scale3 = one step's change of U, V, S (the dU, dV, dS inputs);
+ * out_scale3 = the outputs' unit: the deviation of the next level's U, V, S
+ * from the linear extrapolation.  A NULL array keeps its scales. */
+rg_status rg_mlp_set_scales(rg_mlp* mlp, const float* in_ref3, const float* step_scale3, const float* out_scale3);
 rg_status rg_mlp_get_params(rg_mlp* mlp, float* params);
 rg_status rg_mlp_set_params(rg_mlp* mlp, const float* params);
 
@@ -64,14 +68,14 @@ rg_status rg_mlp_features(rg_mlp* mlp, int n, const int* nodes, const double* U1
                           double q_prev, float* X_out);
 
 /* Append the wet nodes of one time-level triple (levels 2, 1 and the solved
- * level 0) to the training set: features from levels 1 and 2, target the
- * change from level 1 to level 0 divided by the output scales.  wet1 / wet0
- * flag the nodes wet at levels 1 and 0 (nonzero = wet); only nodes wet at
- * both are added.  *added receives the number of samples appended. */
+ * level 0) to the training set: features from levels 1 and 2, target
+ * (level 0 - extrapolation) / output scales.  wet2 / wet1 / wet0 flag the
+ * nodes wet at each level (nonzero = wet); nodes wet at levels 1 and 0 are
+ * added.  *added receives the number of samples appended. */
 rg_status rg_mlp_add_samples(rg_mlp* mlp, const double* U2, const double* V2, const double* S2, const double* U1,
                              const double* V1, const double* S1, const double* U0, const double* V0,
-                             const double* S0, const int* wet1, const int* wet0, double q_next, double q_prev,
-                             long long* added);
+                             const double* S0, const int* wet2, const int* wet1, const int* wet0, double q_next,
+                             double q_prev, long long* added);
 rg_status rg_mlp_clear_samples(rg_mlp* mlp);
 
 /* Adam on the mean squared error over the training set: `epochs` passes in
@@ -85,11 +89,12 @@ rg_status rg_mlp_train(rg_mlp* mlp, int epochs, int batch, float lr, unsigned se
 rg_status rg_mlp_loss_grad(rg_mlp* mlp, int n, const float* X, const float* T, const float* mask, double* loss,
                            float* y_out, float* grad_out);
 
-/* Predicted next time level: wet1 flags the nodes wet at level 1; for those,
- * U/V/S_out = level 1 + predicted change; other nodes copy level 1. */
+/* Predicted next time level: for the nodes wet at level 1, U/V/S_out =
+ * extrapolation (2 L1 - L2, or L1 where wet2 is zero) + outputs x output
+ * scales; other nodes copy level 1. */
 rg_status rg_mlp_predict(rg_mlp* mlp, const double* U2, const double* V2, const double* S2, const double* U1,
-                         const double* V1, const double* S1, const int* wet1, double q_next, double q_prev,
-                         double* U_out, double* V_out, double* S_out);
+                         const double* V1, const double* S1, const int* wet2, const int* wet1, double q_next,
+                         double q_prev, double* U_out, double* V_out, double* S_out);
 
 #ifdef __cplusplus
 }

@@ -116,7 +116,8 @@ rg_status rg_sim_step(rg_sim* sim, double t, double dt, const rg_step_ctl* ctl, 
 /* Starting state of the next rg_sim_step's Newton iteration (e.g. the learned
  * prediction of include/rg300_mlp.h), used once: after the step's first
  * dry/rewet pass it replaces U, V, S on the wet nodes (mid-side S as corner
- * means, depth at least half the dry limit), and is kept only if its residual
+ * means, depth at least half the dry limit, velocity at slip-wall and inlet
+ * nodes projected onto the free direction), and is kept only if its residual
  * ||B|| is below that of the last time level; the step's ||B_0|| stays the
  * last time level's, so the convergence target is unchanged.  NULL arrays
  * cancel a pending start.  No counterpart in the reference

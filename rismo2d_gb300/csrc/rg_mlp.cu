@@ -3,7 +3,9 @@
 // fp32 accumulation), its backward pass and Adam in fp32.
 //
 // Network per node: x (128, bf16) -> [W1 x + b1 -> gelu -> bf16] -> [W2 ...]
-// -> [W3 ...] -> W4 h3 + b4 (3 outputs).  Weights live as fp32 masters and a
+// -> [W3 ...] -> W4 h3 + b4 (3 outputs).  The outputs are the deviation of
+// the next time level from the linear extrapolation 2 L1 - L2 of the last
+// two, in units of the output scales.  Weights live as fp32 masters and a
 // bf16 copy used by every product; the backward pass differentiates the
 // computed function with the bf16 roundings taken as identity.
 
@@ -53,12 +55,13 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1
 }
 
 // ---- features ---------------------------------------------------------------
-// per stencil slot s (node m): dz, H1, U1, V1, dS, dU, dV, distance; then
-// q_next - 1, q_prev - 1 (x10), zeros.  Missing slots are zero.
+// per stencil slot s (node m): dz, H1, U1, V1, dS, dU, dV (level 1 - level 2
+// over the step scales), distance; then q_next - 1, q_prev - 1 (x10), zeros.
+// Missing slots are zero.
 __global__ void k_features(int n, const int* __restrict__ nodes, const int* __restrict__ stencil,
                            const float* __restrict__ dist, const double* __restrict__ zb,
                            const double* __restrict__ st,   // 6 x np: U1 V1 S1 U2 V2 S2
-                           int np, float href, float uref, float zref, float osU, float osV, float osS,
+                           int np, float href, float uref, float zref, float ssU, float ssV, float ssS,
                            float qn, float qp, __nv_bfloat16* __restrict__ X) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * D;
        t += (long long)gridDim.x * blockDim.x) {
@@ -80,9 +83,9 @@ __global__ void k_features(int n, const int* __restrict__ nodes, const int* __re
           case 1: v = (float)(fmax(S1[m] - zb[m], 0.0) / href); break;
           case 2: v = (float)(U1[m] / uref); break;
           case 3: v = (float)(V1[m] / uref); break;
-          case 4: v = (float)((S1[m] - S2[m]) / osS); break;
-          case 5: v = (float)((U1[m] - U2[m]) / osU); break;
-          case 6: v = (float)((V1[m] - V2[m]) / osV); break;
+          case 4: v = (float)((S1[m] - S2[m]) / ssS); break;
+          case 5: v = (float)((U1[m] - U2[m]) / ssU); break;
+          case 6: v = (float)((V1[m] - V2[m]) / ssV); break;
           default: v = dist[(size_t)nd * K + s]; break;
         }
       }
@@ -361,14 +364,23 @@ __global__ void k_to_bf16(const float* __restrict__ P, __nv_bfloat16* __restrict
   }
 }
 
-// targets and mask of appended samples; st: U1 V1 S1 U2 V2 S2 U0 V0 S0 (9 x np)
+// the base of a prediction: 2 L1 - L2 where the node was wet at both levels, else L1
+__host__ __device__ inline double extrapolate(double l1, double l2, bool wet2) { return wet2 ? 2.0 * l1 - l2 : l1; }
+
+// targets and mask of appended samples; st: U1 V1 S1 U2 V2 S2 U0 V0 S0 (9 x np);
+// target = (L0 - base) / output scale
 __global__ void k_targets(int n, const int* __restrict__ nodes, const double* __restrict__ st, int np,
-                          float osU, float osV, float osS, float* __restrict__ T, float* __restrict__ M) {
+                          const int* __restrict__ wet2, float osU, float osV, float osS, float* __restrict__ T,
+                          float* __restrict__ M) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     const int nd = nodes[r];
-    T[(size_t)r * 4 + 0] = (float)((st[6 * (size_t)np + nd] - st[nd]) / osU);
-    T[(size_t)r * 4 + 1] = (float)((st[7 * (size_t)np + nd] - st[(size_t)np + nd]) / osV);
-    T[(size_t)r * 4 + 2] = (float)((st[8 * (size_t)np + nd] - st[2 * (size_t)np + nd]) / osS);
+    const bool w2 = wet2[nd] != 0;
+    const float os[3] = {osU, osV, osS};
+    for (int j = 0; j < 3; j++) {
+      const double l1 = st[(size_t)j * np + nd], l2 = st[(size_t)(3 + j) * np + nd];
+      const double l0 = st[(size_t)(6 + j) * np + nd];
+      T[(size_t)r * 4 + j] = (float)((l0 - extrapolate(l1, l2, w2)) / os[j]);
+    }
     T[(size_t)r * 4 + 3] = 0.0f;
     M[r] = 1.0f;
   }
@@ -386,7 +398,8 @@ struct rg_mlp {
   DBuf<float> dist;
   DBuf<double> zb;
   float in_ref[3] = {4.0f, 1.0f, 1.0f};
-  float out_scale[3] = {0.01f, 0.01f, 0.001f};
+  float step_scale[3] = {0.01f, 0.01f, 0.001f};
+  float out_scale[3] = {0.002f, 0.002f, 0.0002f};
   DBuf<float> P, G, M1, M2;
   DBuf<__nv_bfloat16> Wb;
   int adam_t = 0;
@@ -396,7 +409,7 @@ struct rg_mlp {
   long long nsamp = 0;
   // scratch
   DBuf<double> sstate;
-  DBuf<int> snodes, srows;
+  DBuf<int> snodes, srows, swet;
   DBuf<__nv_bfloat16> sX, sH;
   DBuf<float> sY, sZ, sdY, sdA, sdB, spart, sT, sM;
   DBuf<double> slp;
@@ -509,7 +522,7 @@ rg_status build_features(rg_mlp* m, int n, const int* nodes, const double* const
     MTRY(cudaMemcpyAsync(m->snodes.p, nodes, n * sizeof(int), cudaMemcpyHostToDevice, m->st));
     k_features<<<grid_of(m, (long long)n * D, 256), 256, 0, m->st>>>(
         n, m->snodes.p, m->stencil.p, m->dist.p, m->zb.p, m->sstate.p, np, m->in_ref[0], m->in_ref[1], m->in_ref[2],
-        m->out_scale[0], m->out_scale[1], m->out_scale[2], (float)qn, (float)qp, m->sX.p);
+        m->step_scale[0], m->step_scale[1], m->step_scale[2], (float)qn, (float)qp, m->sX.p);
     MTRY(cudaGetLastError());
   }
   return RG_OK;
@@ -581,12 +594,18 @@ rg_status rg_mlp_get_params(rg_mlp* m, float* params) {
   return RG_OK;
 }
 
-rg_status rg_mlp_set_scales(rg_mlp* m, const float* in_ref3, const float* out_scale3) {
+rg_status rg_mlp_set_scales(rg_mlp* m, const float* in_ref3, const float* step_scale3, const float* out_scale3) {
   if (!m) return RG_ERR_ARG;
   for (int i = 0; i < 3; i++) {
+    const float a = in_ref3 ? in_ref3[i] : m->in_ref[i];
+    const float b = step_scale3 ? step_scale3[i] : m->step_scale[i];
+    const float c = out_scale3 ? out_scale3[i] : m->out_scale[i];
+    if (!(a > 0.0f) || !(b > 0.0f) || !(c > 0.0f)) return mfail(m, RG_ERR_ARG, "scales must be positive");
+  }
+  for (int i = 0; i < 3; i++) {
     if (in_ref3) m->in_ref[i] = in_ref3[i];
+    if (step_scale3) m->step_scale[i] = step_scale3[i];
     if (out_scale3) m->out_scale[i] = out_scale3[i];
-    if (!(m->in_ref[i] > 0.0f) || !(m->out_scale[i] > 0.0f)) return mfail(m, RG_ERR_ARG, "scales must be positive");
   }
   return RG_OK;
 }
@@ -660,8 +679,9 @@ rg_status rg_mlp_clear_samples(rg_mlp* m) {
 
 rg_status rg_mlp_add_samples(rg_mlp* m, const double* U2, const double* V2, const double* S2, const double* U1,
                              const double* V1, const double* S1, const double* U0, const double* V0, const double* S0,
-                             const int* wet1, const int* wet0, double q_next, double q_prev, long long* added) {
-  if (!m || m->np == 0 || !U2 || !V2 || !S2 || !U1 || !V1 || !S1 || !U0 || !V0 || !S0 || !wet1 || !wet0)
+                             const int* wet2, const int* wet1, const int* wet0, double q_next, double q_prev,
+                             long long* added) {
+  if (!m || m->np == 0 || !U2 || !V2 || !S2 || !U1 || !V1 || !S1 || !U0 || !V0 || !S0 || !wet2 || !wet1 || !wet0)
     return RG_ERR_ARG;
   MTRY(cudaSetDevice(m->device));
   std::vector<int> nodes;
@@ -694,8 +714,10 @@ rg_status rg_mlp_add_samples(rg_mlp* m, const double* U2, const double* V2, cons
     std::swap(m->Mk.n, M2.n);
   }
   if (n > 0) {
+    MTRY(ensure(m->swet, (size_t)m->np));
+    MTRY(cudaMemcpyAsync(m->swet.p, wet2, (size_t)m->np * sizeof(int), cudaMemcpyHostToDevice, m->st));
     MTRY(cudaMemcpyAsync(m->X.p + (size_t)m->nsamp * D, m->sX.p, (size_t)n * D * 2, cudaMemcpyDeviceToDevice, m->st));
-    k_targets<<<grid_of(m, n, 256), 256, 0, m->st>>>(n, m->snodes.p, m->sstate.p, m->np, m->out_scale[0],
+    k_targets<<<grid_of(m, n, 256), 256, 0, m->st>>>(n, m->snodes.p, m->sstate.p, m->np, m->swet.p, m->out_scale[0],
                                                      m->out_scale[1], m->out_scale[2], m->T.p + (size_t)m->nsamp * 4,
                                                      m->Mk.p + m->nsamp);
     MTRY(cudaGetLastError());
@@ -785,9 +807,9 @@ rg_status rg_mlp_loss_grad(rg_mlp* m, int n, const float* X, const float* T, con
 }
 
 rg_status rg_mlp_predict(rg_mlp* m, const double* U2, const double* V2, const double* S2, const double* U1,
-                         const double* V1, const double* S1, const int* wet1, double q_next, double q_prev,
-                         double* U_out, double* V_out, double* S_out) {
-  if (!m || m->np == 0 || !U2 || !V2 || !S2 || !U1 || !V1 || !S1 || !wet1 || !U_out || !V_out || !S_out)
+                         const double* V1, const double* S1, const int* wet2, const int* wet1, double q_next,
+                         double q_prev, double* U_out, double* V_out, double* S_out) {
+  if (!m || m->np == 0 || !U2 || !V2 || !S2 || !U1 || !V1 || !S1 || !wet2 || !wet1 || !U_out || !V_out || !S_out)
     return RG_ERR_ARG;
   MTRY(cudaSetDevice(m->device));
   const int np = m->np;
@@ -812,9 +834,10 @@ rg_status rg_mlp_predict(rg_mlp* m, const double* U2, const double* V2, const do
   }
   for (int r = 0; r < n; r++) {
     const int nd = nodes[r];
-    U_out[nd] = U1[nd] + (double)y[(size_t)r * 4 + 0] * m->out_scale[0];
-    V_out[nd] = V1[nd] + (double)y[(size_t)r * 4 + 1] * m->out_scale[1];
-    S_out[nd] = S1[nd] + (double)y[(size_t)r * 4 + 2] * m->out_scale[2];
+    const bool w2 = wet2[nd] != 0;
+    U_out[nd] = extrapolate(U1[nd], U2[nd], w2) + (double)y[(size_t)r * 4 + 0] * m->out_scale[0];
+    V_out[nd] = extrapolate(V1[nd], V2[nd], w2) + (double)y[(size_t)r * 4 + 1] * m->out_scale[1];
+    S_out[nd] = extrapolate(S1[nd], S2[nd], w2) + (double)y[(size_t)r * 4 + 2] * m->out_scale[2];
   }
   return RG_OK;
 }

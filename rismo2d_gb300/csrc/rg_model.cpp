@@ -1145,6 +1145,17 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
         s->V[n] = s->wV[n];
         s->S[n] = std::max(s->wS[n], s->z[n] + 0.5 * s->p.dry_limit);
       }
+      // the fixed velocity component of slip-wall and inlet nodes is no Newton unknown:
+      // project the prediction onto the free direction as GRID::SetSlipFlow does
+      // (SlipFlow.cpp:42-80) for the last time level, so the fixed value stays the plain one
+      for (int n : s->mnodes) {
+        if (!(s->nflag[n] & N_ROTAT)) continue;
+        double r[4];
+        getrot(s, n, r);
+        const double Ut = r[0] * s->U[n] + r[2] * s->V[n];
+        s->U[n] = r[0] * Ut;
+        s->V[n] = r[2] * Ut;
+      }
       for (int e = 0; e < s->ne; e++) {   // mid-side S as the corner mean (k_upd_midside)
         if (s->eflag[e] & E_DRY) continue;
         const int* nd = &s->en[6 * e];

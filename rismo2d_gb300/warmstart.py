@@ -54,7 +54,8 @@ class WarmStartNet:
         en = np.ascontiguousarray(mesh.elems, np.int32).reshape(-1)
         self._check(self.lib.rg_mlp_set_mesh(self.ptr, C.c_int(self.np), p(x), p(y), p(z),
                                              C.c_int(len(en) // 6), p(en)), "rg_mlp_set_mesh")
-        self.out_scale = (0.01, 0.01, 0.001)
+        self.step_scale = (0.01, 0.01, 0.001)
+        self.out_scale = (0.002, 0.002, 0.0002)
 
     def _check(self, st, what):
         if st != _lib.RG_OK:
@@ -71,8 +72,10 @@ class WarmStartNet:
         except Exception:
             pass
 
-    def set_scales(self, in_ref=(4.0, 1.0, 1.0), out_scale=(0.01, 0.01, 0.001)):
-        self._check(self.lib.rg_mlp_set_scales(self.ptr, p(_f32(in_ref)), p(_f32(out_scale))), "rg_mlp_set_scales")
+    def set_scales(self, in_ref=(4.0, 1.0, 1.0), step_scale=(0.01, 0.01, 0.001), out_scale=(0.002, 0.002, 0.0002)):
+        self._check(self.lib.rg_mlp_set_scales(self.ptr, p(_f32(in_ref)), p(_f32(step_scale)), p(_f32(out_scale))),
+                    "rg_mlp_set_scales")
+        self.step_scale = tuple(float(v) for v in step_scale)
         self.out_scale = tuple(float(v) for v in out_scale)
 
     def params(self) -> np.ndarray:
@@ -96,8 +99,8 @@ class WarmStartNet:
         added = C.c_longlong()
         self._check(self.lib.rg_mlp_add_samples(
             self.ptr, p(_f64(s2["U"])), p(_f64(s2["V"])), p(_f64(s2["S"])), p(_f64(s1["U"])), p(_f64(s1["V"])),
-            p(_f64(s1["S"])), p(_f64(s0["U"])), p(_f64(s0["V"])), p(_f64(s0["S"])), p(wet(s1)), p(wet(s0)),
-            C.c_double(q_next), C.c_double(q_prev), C.byref(added)), "rg_mlp_add_samples")
+            p(_f64(s1["S"])), p(_f64(s0["U"])), p(_f64(s0["V"])), p(_f64(s0["S"])), p(wet(s2)), p(wet(s1)),
+            p(wet(s0)), C.c_double(q_next), C.c_double(q_prev), C.byref(added)), "rg_mlp_add_samples")
         return added.value
 
     def clear_samples(self):
@@ -122,20 +125,28 @@ class WarmStartNet:
     def predict(self, s2: dict, s1: dict, q_next: float, q_prev: float):
         U, V, S = (np.zeros(self.np) for _ in range(3))
         self._check(self.lib.rg_mlp_predict(self.ptr, p(_f64(s2["U"])), p(_f64(s2["V"])), p(_f64(s2["S"])),
-                                            p(_f64(s1["U"])), p(_f64(s1["V"])), p(_f64(s1["S"])), p(wet(s1)),
-                                            C.c_double(q_next), C.c_double(q_prev), p(U), p(V), p(S)),
+                                            p(_f64(s1["U"])), p(_f64(s1["V"])), p(_f64(s1["S"])), p(wet(s2)),
+                                            p(wet(s1)), C.c_double(q_next), C.c_double(q_prev), p(U), p(V), p(S)),
                     "rg_mlp_predict")
         return U, V, S
 
 
-def output_scales(states: list) -> tuple:
-    """Standard deviation of one step's change of U, V, S over the wet nodes of a trajectory."""
+def trajectory_scales(states: list) -> tuple:
+    """(step_scale, out_scale) of a trajectory: the RMS over its wet nodes of one
+    step's change of U, V, S, and of the next level's deviation from the linear
+    extrapolation of the last two."""
     d = {v: [] for v in ("U", "V", "S")}
+    e = {v: [] for v in ("U", "V", "S")}
     for a, b in zip(states[:-1], states[1:]):
         w = (wet(a) & wet(b)).astype(bool)
         for v in d:
             d[v].append(b[v][w] - a[v][w])
-    return tuple(max(float(np.std(np.concatenate(d[v]))), 1e-5) for v in ("U", "V", "S"))
+    for a, b, c in zip(states[:-2], states[1:-1], states[2:]):
+        w = (wet(a) & wet(b) & wet(c)).astype(bool)
+        for v in e:
+            e[v].append(c[v][w] - 2.0 * b[v][w] + a[v][w])
+    rms = lambda xs, floor: max(float(np.sqrt(np.mean(np.square(np.concatenate(xs))))), floor)
+    return (tuple(rms(d[v], 1e-6) for v in ("U", "V", "S")), tuple(rms(e[v], 1e-7) for v in ("U", "V", "S")))
 
 
 def collect_trajectory(sim, hydrograph, t0: float, dt: float, nsteps: int, **step_kw) -> tuple:
