@@ -52,11 +52,11 @@ PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 # Newton and Krylov iterations per time step of the plain FP64 GPU path on this
-# workload (first time steps, measured on GB300: 38 / 893 and 35 / 830); used
-# only to scale the CPU solver's per-iteration time when the FP64 arm does not
-# run in the same process.
-FP64_NEWTON_PER_STEP = 36.5
-FP64_KRYLOV_PER_STEP = 861.5
+# workload's first timed steps (time steps 4 and 5, after 3 warm-up steps;
+# measured on GB300: 33 / 801 per step); used only to scale the CPU solver's
+# per-iteration time when the FP64 arm does not run in the same process.
+FP64_NEWTON_PER_STEP = 33.0
+FP64_KRYLOV_PER_STEP = 801.0
 
 # DRAM bytes (read + write) of one k_trsv_wave<float, LOWER> launch on this
 # workload, from the ncu capture summarised in
