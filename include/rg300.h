@@ -116,7 +116,10 @@ rg_status rg_load_system(rg_ctx* ctx, const float* A32, const double* A64, const
 rg_status rg_scale(rg_ctx* ctx, double* scale);
 
 /* PRECO_ILU0::Factor (Preco_ilu0.cpp:64-189) of the resident matrix.
- * Optional output of the factors in the packed layout. */
+ * Optional output of the factors in the packed layout.  The factors stay
+ * resident until the next factorisation or pattern: rg_ilu0_apply and
+ * rg_bicgstab after a new rg_assemble / rg_load_system without a new
+ * rg_ilu0_factor precondition with the factors of the earlier matrix. */
 rg_status rg_ilu0_factor(rg_ctx* ctx, float* LU32_out, double* LU64_out);
 
 /* PRECO_ILU0::Solve (Preco_ilu0.cpp:497-980) of a host vector. */

@@ -82,6 +82,17 @@ typedef struct {
   int    criterion;            /* rg_criterion */
   double residual_tol;
   int    max_newton;           /* 0: params.max_newton */
+  /* 0: every Newton iteration's BiCGStab runs to $SOLVER maxDiff (the
+   * reference).  > 0: inexact Newton -- BiCGStab stops at the relative
+   * residual max(maxDiff, linear_forcing); the Newton convergence test and
+   * the converged solution are unchanged, the path to it takes fewer Krylov
+   * iterations.  No counterpart in the reference. */
+  double linear_forcing;
+  /* 0: ILU(0) is factored in every Newton iteration (the reference).  n > 0:
+   * the resident factors precondition up to n further Newton iterations (also
+   * across time steps) while the numbering is unchanged; a solve that misses
+   * its tolerance forces fresh factors.  No counterpart in the reference. */
+  int    ilu_reuse;
 } rg_step_ctl;
 
 typedef struct {

@@ -720,8 +720,7 @@ rg_status rg_assemble(rg_ctx* c, double* B_out, float* A32_out, double* A64_out)
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
   c->t_ms[0] = ms;
-  c->have_system = true;
-  c->have_factor = false;
+  c->have_system = true;   // resident factors (if any) now belong to an earlier matrix of this pattern
   return copy_out_system(c, B_out, A32_out, A64_out, false);
 }
 
@@ -749,7 +748,6 @@ rg_status rg_load_system(rg_ctx* c, const float* A32, const double* A64, const d
   TRY(rg_copy(c, c->B.p, B, c->neq * sizeof(double), cudaMemcpyHostToDevice));
   TRY(cudaStreamSynchronize(c->st));
   c->have_system = true;
-  c->have_factor = false;
   return RG_OK;
 }
 

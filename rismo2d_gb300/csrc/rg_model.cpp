@@ -137,6 +137,8 @@ struct rg_sim {
   // warm start of the next step (rg_sim_set_warm_start)
   bool warm_pending = false;
   std::vector<double> wU, wV, wS;
+  // ILU(0) reuse (rg_step_ctl::ilu_reuse): numbering generation and age of the resident factors
+  int factor_eqs = -1, factor_age = 0;
 };
 
 static rg_status sfail(rg_sim* s, rg_status st, const std::string& m) {
@@ -890,6 +892,7 @@ rg_status rg_sim_set_state(rg_sim* s, const double* U, const double* V, const do
   set_location(s);
   s->have_state = true;
   s->eqs_init = -1;
+  s->factor_eqs = -1;
   return RG_OK;
 }
 
@@ -1188,14 +1191,25 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       break;
     }
     STAGE("factor");
-    st = rg_ilu0_factor(s->ctx, nullptr, nullptr);
-    if (st != RG_OK) return st;
+    if (ctl->ilu_reuse <= 0 || s->factor_eqs != s->eqs_init || s->factor_age >= ctl->ilu_reuse) {
+      st = rg_ilu0_factor(s->ctx, nullptr, nullptr);
+      if (st != RG_OK) return st;
+      s->factor_eqs = s->eqs_init;
+      s->factor_age = 0;
+    } else {
+      s->factor_age++;   // the factors of an earlier Newton iteration precondition this one
+    }
     STAGE("bicgstab");
     int its = 0;
-    st = rg_bicgstab(s->ctx, s->p.solver_maxiter, s->p.solver_maxdiff, nullptr, &its, nullptr);
+    // inexact Newton on request: the linear solve only as accurate as the forcing term
+    const double lin_tol = std::max(s->p.solver_maxdiff, ctl->linear_forcing);
+    st = rg_bicgstab(s->ctx, s->p.solver_maxiter, lin_tol, nullptr, &its, nullptr);
     krylov_total += its;
     if (st != RG_OK && st != RG_NOT_CONVERGED) return st;
-    if (st == RG_NOT_CONVERGED) status_solve = RG_NOT_CONVERGED;
+    if (st == RG_NOT_CONVERGED) {
+      status_solve = RG_NOT_CONVERGED;
+      s->factor_eqs = -1;   // fresh factors for the next iteration
+    }
     double stats[6];
     STAGE("update");
     st = rg_newton_update(s->ctx, &uo, stats);

@@ -43,7 +43,8 @@ class Deck(C.Structure):
 
 class StepCtl(C.Structure):
     _fields_ = [("steady", C.c_int), ("first_step", C.c_int), ("criterion", C.c_int),
-                ("residual_tol", C.c_double), ("max_newton", C.c_int)]
+                ("residual_tol", C.c_double), ("max_newton", C.c_int), ("linear_forcing", C.c_double),
+                ("ilu_reuse", C.c_int)]
 
 
 class StepReport(C.Structure):
@@ -179,8 +180,10 @@ class Simulation:
         return out
 
     def step(self, t: float, dt: float, steady: bool = False, criterion: int = RG_CRIT_RESIDUAL,
-             residual_tol: float = 1e-8, max_newton: int = 0) -> dict:
-        ctl = StepCtl(1 if steady else 0, 1 if self.step_no == 0 else 0, criterion, residual_tol, max_newton)
+             residual_tol: float = 1e-8, max_newton: int = 0, linear_forcing: float = 0.0,
+             ilu_reuse: int = 0) -> dict:
+        ctl = StepCtl(1 if steady else 0, 1 if self.step_no == 0 else 0, criterion, residual_tol, max_newton,
+                      linear_forcing, ilu_reuse)
         rep = StepReport()
         st = self.lib.rg_sim_step(self.ptr, C.c_double(t), C.c_double(dt), C.byref(ctl), C.byref(rep))
         if st not in (_lib.RG_OK, _lib.RG_NOT_CONVERGED):
