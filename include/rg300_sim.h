@@ -134,6 +134,24 @@ rg_status rg_sim_step(rg_sim* sim, double t, double dt, const rg_step_ctl* ctl, 
  * cancel a pending start.  No counterpart in the reference
  * (EQS_UVS2D::Predict, EqsUVS2D.cpp:1101, starts from the last time level). */
 rg_status rg_sim_set_warm_start(rg_sim* sim, const double* U, const double* V, const double* S);
+/* host wall time of the stages of rg_sim_step since the last reset, in ms
+ * (indices rg_sim_stage; device work is included where the stage waits for
+ * it).  ms[0..n-1] receive the sums; reset != 0 zeroes them afterwards. */
+typedef enum {
+  RG_STAGE_DRYREWET = 0,       /* dry/rewet passes on the host */
+  RG_STAGE_FRICTION = 1,       /* nodal friction (GPU) */
+  RG_STAGE_BCON = 2,           /* boundary conditions, location, normals, rotation (host) */
+  RG_STAGE_NUMBERING = 3,      /* numbering and pattern after a model change (host) */
+  RG_STAGE_UPLOAD = 4,         /* state, model and boundary uploads */
+  RG_STAGE_DOWNLOAD = 5,       /* state downloads */
+  RG_STAGE_ASSEMBLE = 6,       /* assembly and scaling (GPU) */
+  RG_STAGE_FACTOR = 7,         /* ILU(0) factorisation (GPU) */
+  RG_STAGE_KRYLOV = 8,         /* BiCGStab (GPU) */
+  RG_STAGE_UPDATE = 9,         /* Newton update and time derivatives (GPU) */
+  RG_STAGE_WARM = 10,          /* warm start: applying and testing the predicted start */
+  RG_SIM_NSTAGE = 11
+} rg_sim_stage;
+rg_status rg_sim_stage_ms(rg_sim* sim, double* ms, int n, int reset);
 /* the host part of one Newton iteration's set-up with the given nodal
  * friction (InitBcon at time t_bc, SetLocation, SetNormal, SetRotation,
  * SetEqno when the model changed) -- no GPU work */

@@ -40,7 +40,7 @@ EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pat
            "rg_mlp_create", "rg_mlp_destroy", "rg_mlp_last_error", "rg_mlp_set_mesh", "rg_mlp_set_scales",
            "rg_mlp_get_params", "rg_mlp_set_params", "rg_mlp_features", "rg_mlp_add_samples",
            "rg_mlp_clear_samples", "rg_mlp_train", "rg_mlp_loss_grad", "rg_mlp_predict",
-           "rg_sim_set_warm_start"]
+           "rg_sim_set_warm_start", "rg_sim_stage_ms"]
 
 
 class RgMesh(C.Structure):

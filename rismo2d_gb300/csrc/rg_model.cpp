@@ -139,7 +139,29 @@ struct rg_sim {
   std::vector<double> wU, wV, wS;
   // ILU(0) reuse (rg_step_ctl::ilu_reuse): numbering generation and age of the resident factors
   int factor_eqs = -1, factor_age = 0;
+  // boundary set-up cache: within one time step and one wet model the node
+  // kinds, normals and rotations repeat; only the inlet values (friction,
+  // dryness) change from one Newton iteration to the next
+  bool bc_valid = false;
+  std::vector<int> line_nodes;   // nodes of the control lines, ascending
+  std::vector<int> zero_uv;      // kNoMoment nodes of the last full set-up
+  std::vector<unsigned> ib_kind; // init_bcon work arrays (line nodes only are touched)
+  std::vector<char> ib_has, ib_mark;
+  std::vector<double> ib_vU, ib_vS;
+  // host wall time per stage of rg_sim_step (rg_sim_stage_ms)
+  double stage_ms[RG_SIM_NSTAGE] = {};
+  int stage_cur = -1;
+  std::chrono::steady_clock::time_point stage_t0;
 };
+
+// close the running stage of rg_sim_step and start stage `next` (-1: none)
+static void stage_switch(rg_sim* s, int next) {
+  const auto now = std::chrono::steady_clock::now();
+  if (s->stage_cur >= 0)
+    s->stage_ms[s->stage_cur] += std::chrono::duration<double, std::milli>(now - s->stage_t0).count();
+  s->stage_cur = next;
+  s->stage_t0 = now;
+}
 
 static rg_status sfail(rg_sim* s, rg_status st, const std::string& m) {
   s->err = m;
@@ -348,15 +370,32 @@ static void getrot(const rg_sim* s, int n, double r[4]) {
 // ---- BCONSET::InitBcon ------------------------------------------------------
 
 // returns true when the inlet was dry and its water level was initialised
-static bool init_bcon(rg_sim* s, double t) {
+// values_only: the node kinds and BCVAL::S are those of the last full call
+// (same time, same wet model); only BCVAL::U (and S of a dry inlet) are
+// recomputed, for the control-line nodes -- the same values a full call gives
+static bool init_bcon(rg_sim* s, double t, bool values_only = false) {
   bool s_changed = false;
   const int np = s->np;
-  std::vector<unsigned> kind(np, 0);
-  std::vector<char> has(np, 0);
-  std::vector<double> vU(np, 0.0), vS(np, 0.0);
-  std::vector<char> mark(np, 0);
+  std::vector<unsigned>& kind = s->ib_kind;
+  std::vector<char>& has = s->ib_has;
+  std::vector<double>& vU = s->ib_vU;
+  std::vector<double>& vS = s->ib_vS;
+  std::vector<char>& mark = s->ib_mark;
+  if ((int)kind.size() != np) {
+    kind.assign(np, 0);
+    has.assign(np, 0);
+    vU.assign(np, 0.0);
+    vS.assign(np, 0.0);
+    mark.assign(np, 0);
+  }
+  // only control-line nodes are ever written
+  for (int n : s->line_nodes) {
+    kind[n] = 0;
+    has[n] = 0;
+    vU[n] = vS[n] = 0.0;
+  }
   for (const LineBc& b : s->bcl) {
-    std::fill(mark.begin(), mark.end(), 0);
+    for (int n : s->line_nodes) mark[n] = 0;
     unsigned k = b.kind;
     if (k & B_QTINLET) k |= B_QINLET;
     if (k & B_QINLET) k |= B_INLET;
@@ -420,7 +459,7 @@ static bool init_bcon(rg_sim* s, double t) {
         Qratio = (std::fabs(Q) > 0.0) ? (-Qspec / Q) : 0.0;
         s_changed = true;
       }
-      for (int n = 0; n < np; n++) {
+      for (int n : s->line_nodes) {
         if (!mark[n]) continue;
         double qn = 0.0;
         if (!(s->nflag[n] & (N_DRY | N_MARSH))) {
@@ -459,6 +498,10 @@ static bool init_bcon(rg_sim* s, double t) {
         }
       }
     }
+  }
+  if (values_only) {
+    for (int n : s->line_nodes) s->bcU[n] = has[n] ? vU[n] : 0.0;
+    return s_changed;
   }
   for (int n = 0; n < np; n++) {
     unsigned k = kind[n];
@@ -716,6 +759,7 @@ static void slip_flow(rg_sim* s) {
 }
 
 static void do_dry_rewet(rg_sim* s, int* del, int* wel) {
+  s->bc_valid = false;
   connection(s, 0);
   *del = *wel = 0;
   if (s->p.dryrew_method == 2) dry_rewet(s, del, wel);
@@ -769,6 +813,9 @@ rg_status rg_sim_create(const rg_deck* d, int precision, int device, rg_sim** ou
   }
   s->seg_nodes.assign(d->seg_nodes, d->seg_nodes + 3 * (size_t)d->nseg);
   s->seg_line.assign(d->seg_line, d->seg_line + d->nseg);
+  s->line_nodes = s->seg_nodes;
+  std::sort(s->line_nodes.begin(), s->line_nodes.end());
+  s->line_nodes.erase(std::unique(s->line_nodes.begin(), s->line_nodes.end()), s->line_nodes.end());
   for (int b = 0; b < d->nbc; b++) {
     const rg_line_bc& lb = d->bc[b];
     LineBc l;
@@ -919,6 +966,7 @@ rg_status rg_sim_dry_rewet(rg_sim* s, int* dried, int* wetted) {
 rg_status rg_sim_prepare_iteration(rg_sim* s, double t_bc, const double* cf) {
   if (!s || !s->have_state) return RG_ERR_ARG;
   if (cf) s->cf.assign(cf, cf + s->np);
+  s->bc_valid = false;
   init_bcon(s, t_bc);
   set_location(s);
   set_normal(s);
@@ -991,6 +1039,15 @@ rg_status rg_sim_get_model(rg_sim* s, int* ne, int* elem_nodes, int* elem_nnd, i
   return RG_OK;
 }
 
+rg_status rg_sim_stage_ms(rg_sim* s, double* ms, int n, int reset) {
+  if (!s || n < 0 || (n > 0 && !ms)) return RG_ERR_ARG;
+  for (int i = 0; i < n && i < RG_SIM_NSTAGE; i++) ms[i] = s->stage_ms[i];
+  for (int i = RG_SIM_NSTAGE; i < n; i++) ms[i] = 0.0;
+  if (reset)
+    for (double& v : s->stage_ms) v = 0.0;
+  return RG_OK;
+}
+
 rg_status rg_sim_set_warm_start(rg_sim* s, const double* U, const double* V, const double* S) {
   if (!s || !s->have_state) return RG_ERR_ARG;
   if (!U || !V || !S) {
@@ -1008,6 +1065,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
   if (!s || !ctl || !s->have_state || dt <= 0.0) return RG_ERR_ARG;
   if (!s->ctx) return sfail(s, RG_ERR_ARG, "rg_sim_step: created without a GPU context");
   auto t0 = std::chrono::steady_clock::now();
+  s->bc_valid = false;   // new boundary time
   const bool steady = ctl->steady != 0;
   const double th = s->p.theta;
   double rUV, rH;
@@ -1055,8 +1113,9 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
   double last_ratio = 1.0;
   const bool trace = getenv("RG_TRACE") != nullptr;
   const bool trace2 = trace && getenv("RG_TRACE")[0] == '2';
-#define STAGE(name)                                          \
+#define STAGE(name, idx)                                     \
   do {                                                       \
+    stage_switch(s, idx);                                    \
     if (trace2) fprintf(stderr, "[rg]   stage %s\n", name); \
   } while (0)
   for (int it = 0; it < maxit; it++) {
@@ -1065,12 +1124,13 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       if (nextDW >= 0 && (it == nextDW || NRconv)) {
         nextDW = it + DWfreq;
         if (state_on_device) {
+          STAGE("pull_state", RG_STAGE_DOWNLOAD);
           st = pull_state(s);
           if (st != RG_OK) return st;
           state_on_device = false;
         }
         int del = 0, wel = 0;
-        STAGE("dry_rewet");
+        STAGE("dry_rewet", RG_STAGE_DRYREWET);
         do_dry_rewet(s, &del, &wel);
         if (trace2) fprintf(stderr, "[rg]   dried %d wetted %d\n", del, wel);
         dw_events++;
@@ -1085,6 +1145,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     }
     NRconv = true;
     if (!state_on_device) {
+      STAGE("push_state", RG_STAGE_UPLOAD);
       st = push_state(s);
       if (st != RG_OK) return st;
       state_on_device = true;
@@ -1094,43 +1155,56 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     auto build_system = [&](double* scale) -> rg_status {
       rg_status st;
       // friction (GPU) and boundary data (host) of this iteration
-      STAGE("friction");
+      STAGE("friction", RG_STAGE_FRICTION);
       st = rg_friction(s->ctx, s->cf.data());
       if (st != RG_OK) return st;
       if (!s->bcl.empty()) {
         // the inlet distribution reads S, z at the inlet nodes: the device copy is current
+        STAGE("inlet_state", RG_STAGE_DOWNLOAD);
         st = rg_get_state(s->ctx, nullptr, nullptr, s->S.data(), s->z.data());
         if (st != RG_OK) return st;
       }
-      STAGE("init_bcon");
-      if (init_bcon(s, t + dt)) {
+      STAGE("init_bcon", RG_STAGE_BCON);
+      // the same time and wet model as the last set-up: kinds, normals and rotations repeat
+      const bool refresh = s->bc_valid && s->eqs_init == s->model_init;
+      if (init_bcon(s, t + dt, refresh)) {
         st = rg_set_state(s->ctx, nullptr, nullptr, s->S.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
                           nullptr);
         if (st != RG_OK) return st;
       }
-      set_location(s);
-      set_normal(s);
-      std::vector<int> zero_uv;
-      set_rotation(s, &zero_uv);
-      if (!zero_uv.empty()) {
-        st = rg_zero_velocity(s->ctx, (int)zero_uv.size(), zero_uv.data());
+      if (refresh) {
+        for (int n : s->zero_uv) s->U[n] = s->V[n] = 0.0;
+      } else {
+        set_location(s);
+        set_normal(s);
+        s->zero_uv.clear();
+        set_rotation(s, &s->zero_uv);
+      }
+      if (!s->zero_uv.empty()) {
+        st = rg_zero_velocity(s->ctx, (int)s->zero_uv.size(), s->zero_uv.data());
         if (st != RG_OK) return st;
       }
       if (s->eqs_init != s->model_init) {
         s->eqs_init = s->model_init;
-        STAGE("set_eqno");
+        STAGE("set_eqno", RG_STAGE_NUMBERING);
         st = set_eqno(s);
         if (st != RG_OK) return st;
-        STAGE("push_model");
+        STAGE("push_model", RG_STAGE_UPLOAD);
         st = push_model(s);
         if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
         st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
         if (st != RG_OK) return st;
       }
-      st = push_boundary(s);
+      STAGE("push_boundary", RG_STAGE_UPLOAD);
+      if (refresh) {
+        st = rg_set_boundary(s->ctx, nullptr, nullptr, nullptr, nullptr, nullptr, s->bcU.data(), nullptr);
+      } else {
+        st = push_boundary(s);
+        s->bc_valid = true;
+      }
       if (st != RG_OK) return st;
       // assemble, scale: ||B_k|| is the Newton residual
-      STAGE("assemble");
+      STAGE("assemble", RG_STAGE_ASSEMBLE);
       st = rg_assemble(s->ctx, nullptr, nullptr, nullptr);
       if (st != RG_OK) return st;
       return rg_scale(s->ctx, scale);
@@ -1139,6 +1213,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     st = build_system(&scale);
     if (st != RG_OK) return st;
     if (it == 0 && s->warm_pending) {
+      STAGE("warm_start", RG_STAGE_WARM);
       // learned warm start: the predicted state replaces the last time level on the
       // wet nodes if its residual is the smaller one; ||B_0|| stays the plain start's
       s->warm_pending = false;
@@ -1190,7 +1265,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       converged = true;
       break;
     }
-    STAGE("factor");
+    STAGE("factor", RG_STAGE_FACTOR);
     if (ctl->ilu_reuse <= 0 || s->factor_eqs != s->eqs_init || s->factor_age >= ctl->ilu_reuse) {
       st = rg_ilu0_factor(s->ctx, nullptr, nullptr);
       if (st != RG_OK) return st;
@@ -1199,7 +1274,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     } else {
       s->factor_age++;   // the factors of an earlier Newton iteration precondition this one
     }
-    STAGE("bicgstab");
+    STAGE("bicgstab", RG_STAGE_KRYLOV);
     int its = 0;
     // inexact Newton on request: the linear solve only as accurate as the forcing term
     const double lin_tol = std::max(s->p.solver_maxdiff, ctl->linear_forcing);
@@ -1211,7 +1286,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       s->factor_eqs = -1;   // fresh factors for the next iteration
     }
     double stats[6];
-    STAGE("update");
+    STAGE("update", RG_STAGE_UPDATE);
     st = rg_newton_update(s->ctx, &uo, stats);
     if (st != RG_OK) return st;
     newton++;
@@ -1220,6 +1295,7 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
               scale, its, (int)st, stats[0], stats[1], stats[2], dw_events);
     if (stats[0] > s->p.conv_uv || stats[1] > s->p.conv_uv || stats[2] > s->p.conv_s) NRconv = false;
     if (!steady) {
+      STAGE("timegrad", RG_STAGE_UPDATE);
       st = rg_timegrad(s->ctx, dt, th);
       if (st != RG_OK) return st;
     }
@@ -1228,10 +1304,12 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       break;
     }
   }
+  STAGE("end_of_step", RG_STAGE_DOWNLOAD);
   if (state_on_device) {
     st = pull_state(s);
     if (st != RG_OK) return st;
   }
+  stage_switch(s, -1);
   // GRID::SetSlipFlow at the end of the step (EqsUVS2D.cpp:1078)
   slip_flow(s);
   // end of the time step (Compute.cpp:774-810)

@@ -191,6 +191,17 @@ class Simulation:
         self.step_no += 1
         return rep.as_dict()
 
+    STAGES = ("dry_rewet", "friction", "bcon", "numbering", "upload", "download", "assemble", "factor", "krylov",
+              "update", "warm_start")
+
+    def stage_ms(self, reset: bool = False) -> dict:
+        """Host wall time per stage of the steps since the last reset (ms)."""
+        ms = np.zeros(len(self.STAGES))
+        st = self.lib.rg_sim_stage_ms(self.ptr, p(ms), C.c_int(len(ms)), C.c_int(1 if reset else 0))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_stage_ms")
+        return dict(zip(self.STAGES, ms.tolist()))
+
     # -- inspection of the host model (numbering, pattern, boundary data) ----
     def prepare_iteration(self, t_bc: float, cf=None):
         cf = None if cf is None else np.ascontiguousarray(cf, np.float64)
