@@ -12,13 +12,18 @@ scaled residual ||B_k|| / ||B_0|| <= 1e-8.
 
 A "step" is one such time step.  Default arm (the headline): the
 mixed-precision solver (FP32 Krylov / SpMV / ILU(0) inside FP64 iterative
-refinement, FP64 residual and update) started from the learned warm start.
+refinement, FP64 residual and update) started from the learned warm start,
+as an inexact Newton iteration (BiCGStab to relative residual 0.1, ILU(0)
+factors reused for up to 16 Newton iterations); the Newton convergence test
+is the same ||B_k|| / ||B_0|| <= 1e-8.
 The network is trained on the GPU, before the timed region, on a trajectory
 of the plain mixed solver under a different hydrograph (Q(t) = 250 + 700
 sin^2(pi t / 5400), 12 steps from rest); the timed steps are held out.  Each
 timed step includes the prediction (features + forward pass, host copies in
-and out).  The same time steps also run cold-started (mixed, no warm start)
-and with the plain FP64 GPU path for comparison; the CPU restatement of the
+and out).  The same time steps also run cold-started (mixed, same Newton-
+Krylov options, no warm start), cold with the reference's linear solves, and
+with the plain FP64 GPU path (the reference's algorithm) for comparison; the
+CPU restatement of the
 reference's solver is timed on a bounded sample on the host cores.
 `--impl reference` times that CPU solver alone.  One JSON line on stdout.
 """
@@ -46,6 +51,10 @@ WORKLOAD = ("meander 10 km x 601 m, 200,028 P2 triangles (402,747 nodes), unstea
 # training trajectory of the warm-start network: another hydrograph, from rest
 TRAIN_HYDROGRAPH = dict(Q0=250.0, dQ=700.0, period=5400.0, t_end=7200.0)
 TRAIN_STEPS = 12
+# Newton-Krylov options of the mixed arms (the FP64 arm runs the reference's
+# linear solves: ILU(0) factored and BiCGStab to maxDiff in every iteration)
+LINEAR_FORCING = 0.1
+ILU_REUSE = 16
 TRAIN_EPOCHS = 30
 TRAIN_BATCH = 8192
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
@@ -196,7 +205,7 @@ def train_net(device: int, max_newton: int = 0):
 
 
 def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, clocks: Clocks | None, dist: Dist,
-            flush_buf, max_newton: int = 0, net=None):
+            flush_buf, max_newton: int = 0, net=None, linear_forcing: float = 0.0, ilu_reuse: int = 0):
     """W warm-up and K timed time steps through Simulation.step; per-step device time by
     CUDA events on the library's stream, host wall time of step + state download.  With
     `net`, every step after the first starts from the network's prediction; the
@@ -221,14 +230,16 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
         # network copies: 6 state arrays + node list in, 4 floats per wet node out
         return (time.perf_counter() - p0) * 1e3, 6 * 8 * mesh.np + 4 * nwet, 16 * nwet
 
+    kw = dict(criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL, max_newton=max_newton,
+              linear_forcing=linear_forcing, ilu_reuse=ilu_reuse)
     for _ in range(warmup):
         predict()
-        reps.append(sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL,
-                             max_newton=max_newton))
+        reps.append(sim.step(t, STEP_DT, **kw))
         t += STEP_DT
         if net:
             hist = [hist[-1], sim.get_state()]
     st0 = sim.stats()
+    sim.stage_ms(reset=True)
     if profile:
         sim.profile(True, reset=True)
     dev_ms, e2e_ms, timed = [], [], []
@@ -246,7 +257,7 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
         pred_h2d += bi
         pred_d2h += bo
         sim.event_record(0)
-        rep = sim.step(t, STEP_DT, criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL, max_newton=max_newton)
+        rep = sim.step(t, STEP_DT, **kw)
         sim.event_record(1)
         state = sim.get_state()               # result to host memory (numpy)
         h1 = time.perf_counter()
@@ -262,13 +273,14 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
     wall1 = time.perf_counter()
     clk = clocks.stop() if clocks else None
     st1 = sim.stats()
+    stage = {k: round(v / steps, 2) for k, v in sim.stage_ms().items()}
     prof = sim.profile_read() if profile else None
     if profile:
         sim.profile(False)
     # the network's launches per prediction: features + forward
     out = dict(dev_ms=dev_ms, e2e_ms=e2e_ms, wall_s=wall1 - wall0, reps=timed, warm_reps=reps, states=states,
                stats=st1.tolist(), h2d=int(st1[12] - st0[12]) + pred_h2d, d2h=int(st1[13] - st0[13]) + pred_d2h,
-               launches=int(st1[14] - st0[14]) + (2 * steps if net else 0), prof=prof, clocks=clk)
+               launches=int(st1[14] - st0[14]) + (2 * steps if net else 0), prof=prof, clocks=clk, stage=stage)
     sim.close()
     return out
 
@@ -407,6 +419,13 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the plain FP64 comparison (0: skip)")
     ap.add_argument("--cold-steps", type=int, default=5,
                     help="timed steps of the mixed solver without warm start (0: skip)")
+    ap.add_argument("--exact-steps", type=int, default=2,
+                    help="timed steps of the mixed solver, cold, with the reference's linear solves: every Newton "
+                         "iteration factors ILU(0) and solves to maxDiff (0: skip)")
+    ap.add_argument("--linear-forcing", type=float, default=LINEAR_FORCING,
+                    help="inexact Newton: BiCGStab to max(maxDiff, this) relative residual (0: maxDiff)")
+    ap.add_argument("--ilu-reuse", type=int, default=ILU_REUSE,
+                    help="Newton iterations an ILU(0) factorisation is reused for (0: factor every iteration)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU solver sampling (0: skip)")
     ap.add_argument("--max-newton", type=int, default=0,
                     help="cap on Newton iterations per step, for short profiling runs only (0: none; a capped "
@@ -447,8 +466,9 @@ def main():
     from rismo2d_gb300 import _lib
     clocks = Clocks(device)
     net, learned_info = train_net(device, args.max_newton)
+    solver_kw = dict(linear_forcing=args.linear_forcing, ilu_reuse=args.ilu_reuse)
     mixed = run_gpu(_lib.PREC_MIXED, warmup, args.steps, device, True, clocks, dist, flush_buf, args.max_newton,
-                    net=net)
+                    net=net, **solver_kw)
     net.close()
     k = args.steps
     dev_s = sum(mixed["dev_ms"]) / 1e3
@@ -472,7 +492,7 @@ def main():
     cold = None
     if args.cold_steps > 0:
         kc = min(args.cold_steps, k)
-        c = run_gpu(_lib.PREC_MIXED, warmup, kc, device, False, None, dist, flush_buf, args.max_newton)
+        c = run_gpu(_lib.PREC_MIXED, warmup, kc, device, False, None, dist, flush_buf, args.max_newton, **solver_kw)
         cs = sum(c["dev_ms"]) / 1e3 / kc
         cold = {"s_per_step": round(cs, 4), "steps": kc,
                 "newton_per_step": statistics.mean(r["newton_iterations"] for r in c["reps"]),
@@ -480,6 +500,15 @@ def main():
                 "converged": all(r["converged"] for r in c["reps"]),
                 "learned_speedup": round(cs / (sum(mixed["dev_ms"][:kc]) / 1e3 / kc), 3),
                 "learned_vs_cold_max_rel_err": rel_errs(mixed["states"][:kc], c["states"])}
+    exact = None
+    if args.exact_steps > 0:
+        ke = min(args.exact_steps, k)
+        x = run_gpu(_lib.PREC_MIXED, warmup, ke, device, False, None, dist, flush_buf, args.max_newton)
+        exact = {"s_per_step": round(sum(x["dev_ms"]) / 1e3 / ke, 4), "steps": ke,
+                 "newton_per_step": statistics.mean(r["newton_iterations"] for r in x["reps"]),
+                 "krylov_per_step": statistics.mean(r["krylov_iterations"] for r in x["reps"]),
+                 "converged": all(r["converged"] for r in x["reps"]),
+                 "host_stage_ms_per_step": x["stage"]}
     fp64 = None
     if args.fp64_steps > 0:
         kf = min(args.fp64_steps, k)
@@ -508,15 +537,20 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov/ILU(0) + f64 refinement",
                 "data": "synthetic (seeded meander mesh, no external dataset)",
                 "config": {"workload": WORKLOAD, "solver": "mixed: FP32 BiCGStab/ILU(0)/SpMV in FP64 iterative "
-                           "refinement, started from the learned warm start (prediction inside each timed step)",
+                           "refinement, started from the learned warm start (prediction inside each timed step); "
+                           f"inexact Newton: BiCGStab to relative residual {args.linear_forcing:g}; ILU(0) factors "
+                           f"reused for up to {args.ilu_reuse} Newton iterations; the Newton test stays "
+                           "||B_k||/||B_0|| <= 1e-8",
                            "precision_arm": "mixed+learned",
+                           "linear_forcing": args.linear_forcing, "ilu_reuse": args.ilu_reuse,
                            "parallelism": "replicas only" if dist.world > 1 else "1 GPU",
                            "l2": "256 MiB buffer written between timed steps (the ~60 MB system stays "
                                  "L2-resident within a step)",
                            "neq": int(st[0]), "nnz": int(st[1])},
                 "newton_per_step": statistics.mean(newton), "krylov_per_step": statistics.mean(krylov),
                 "converged": conv, "warm_start_accepted": sum(r["warm_start"] for r in mixed["reps"]),
-                "learned": learned_info, "cold_start": cold, "fp64": fp64,
+                "learned": learned_info, "cold_start": cold, "mixed_reference_solves": exact, "fp64": fp64,
+                "host_stage_ms_per_step": mixed["stage"],
                 "clocks": mixed["clocks"],
                 "e2e": {"value": round(e2e_s, 4), "unit": "s/step",
                         "h2d_bytes_per_step": mixed["h2d"] // k, "d2h_bytes_per_step": mixed["d2h"] // k,

@@ -460,6 +460,62 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
   }
   TRY(upload(c, c->color_elem, celem.data(), celem.size()));
 
+  // two-phase assembly: element lists and, per CRS entry and per equation, its
+  // contributions in assembly order -- the order the colour-by-colour scatter adds them
+  {
+    const long long nasm = (long long)celem.size();
+    if (nasm * RG_EQ * RG_EQ > 2147483647ll) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: too many elements");
+    std::vector<int> areg, abnd;
+    for (int k = 0; k < ncol; k++) {
+      for (int p = c->color_ptr[3 * k]; p < c->color_ptr[3 * k + 1]; p++) areg.push_back(p);
+      for (int p = c->color_ptr[3 * k + 1]; p < c->color_ptr[3 * k + 2]; p++) abnd.push_back(p);
+    }
+    std::vector<long long> gptr((size_t)nnz + 1, 0), rptr((size_t)neq + 1, 0);
+    for (long long p = 0; p < nasm; p++) {
+      const int e = celem[p];
+      const int nr = (c->h_eflag[e] & RG_E_BOUND) ? 9 : RG_EQ;
+      const int* sl = &slot[(size_t)e * RG_EQ * RG_EQ];
+      for (int r = 0; r < nr; r++) {
+        for (int cc = 0; cc < nr; cc++)
+          if (sl[r * RG_EQ + cc] >= 0) gptr[sl[r * RG_EQ + cc] + 1]++;
+        const int row = erow[(size_t)e * RG_EQ + r];
+        if (row >= 0) rptr[row + 1]++;
+      }
+    }
+    for (size_t q = 0; q < (size_t)nnz; q++) gptr[q + 1] += gptr[q];
+    for (int r = 0; r < neq; r++) rptr[r + 1] += rptr[r];
+    std::vector<int> gsrc((size_t)gptr[nnz]), rsrc((size_t)rptr[neq]);
+    std::vector<long long> gfill(gptr.begin(), gptr.end() - 1), rfill(rptr.begin(), rptr.end() - 1);
+    for (long long p = 0; p < nasm; p++) {
+      const int e = celem[p];
+      const int nr = (c->h_eflag[e] & RG_E_BOUND) ? 9 : RG_EQ;
+      const int* sl = &slot[(size_t)e * RG_EQ * RG_EQ];
+      for (int r = 0; r < nr; r++) {
+        for (int cc = 0; cc < nr; cc++) {
+          const int q = sl[r * RG_EQ + cc];
+          if (q >= 0) gsrc[gfill[q]++] = (int)(p * RG_EQ * RG_EQ + r * RG_EQ + cc);
+        }
+        const int row = erow[(size_t)e * RG_EQ + r];
+        if (row >= 0) rsrc[rfill[row]++] = (int)(p * RG_EQ + r);
+      }
+    }
+    c->n_asm_reg = (int)areg.size();
+    c->n_asm_bnd = (int)abnd.size();
+    TRY(upload(c, c->asm_reg, areg.data(), std::max<size_t>(areg.size(), 1)));
+    TRY(upload(c, c->asm_bnd, abnd.data(), std::max<size_t>(abnd.size(), 1)));
+    TRY(upload(c, c->gat_ptr, gptr.data(), gptr.size()));
+    TRY(upload(c, c->grow_ptr, rptr.data(), rptr.size()));
+    TRY(upload(c, c->gat_src, gsrc.data(), std::max<size_t>(gsrc.size(), 1)));
+    TRY(upload(c, c->grow_src, rsrc.data(), std::max<size_t>(rsrc.size(), 1)));
+    const size_t nk = (size_t)std::max<long long>(nasm, 1) * RG_EQ * RG_EQ;
+    if (c->prec == RG_PREC_MIXED) {
+      TRY(c->EK32.alloc(nk));
+    } else {
+      TRY(c->EK64.alloc(nk));
+    }
+    TRY(c->EF.alloc((size_t)std::max<long long>(nasm, 1) * RG_EQ));
+  }
+
   // ILU(0) schedule: L positions sorted by column; split L/U operands
   std::vector<int> lsp(neq + 1, 0), lspos, Lptr(neq + 1, 0), Lcol, Lsrc, Uptr(neq + 1, 0), Ucol, Usrc;
   std::vector<std::pair<int, int>> tmp;

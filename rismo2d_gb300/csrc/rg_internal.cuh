@@ -152,7 +152,16 @@ struct rg_ctx {
   DBuf<int> slot;            // per element RG_EQ*RG_EQ CRS positions (-1 = none)
   DBuf<int> erow;            // per element RG_EQ equation numbers of its rows
   std::vector<int> color_ptr;
-  DBuf<int> color_elem;      // elements grouped by colour
+  DBuf<int> color_elem;      // elements grouped by colour (the assembly order)
+  // two-phase assembly: element matrices by position in color_elem, then one
+  // gather per CRS entry / equation over its contributions in that order
+  DBuf<int> asm_reg, asm_bnd;        // positions of region triangles / boundary lines
+  int n_asm_reg = 0, n_asm_bnd = 0;
+  DBuf<long long> gat_ptr, grow_ptr; // per CRS entry (nnz + 1) / per equation (neq + 1)
+  DBuf<int> gat_src;                 // position * RG_EQ*RG_EQ + r * RG_EQ + c
+  DBuf<int> grow_src;                // position * RG_EQ + r
+  DBuf<double> EK64, EF;             // element matrices (FP64 Jacobian), element residuals
+  DBuf<float> EK32;                  // element matrices (FP32 Jacobian)
 
   // values
   DBuf<double> A64, LU64;
