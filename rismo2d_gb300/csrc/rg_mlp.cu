@@ -78,14 +78,15 @@ __global__ void k_features(int n, const int* __restrict__ nodes, const int* __re
         const double* U2 = st + 3 * (size_t)np;
         const double* V2 = st + 4 * (size_t)np;
         const double* S2 = st + 5 * (size_t)np;
+        // differences in FP64 (levels and elevations are large numbers), scaling in FP32
         switch (c) {
-          case 0: v = (float)((zb[m] - zb[nd]) / zref); break;
-          case 1: v = (float)(fmax(S1[m] - zb[m], 0.0) / href); break;
-          case 2: v = (float)(U1[m] / uref); break;
-          case 3: v = (float)(V1[m] / uref); break;
-          case 4: v = (float)((S1[m] - S2[m]) / ssS); break;
-          case 5: v = (float)((U1[m] - U2[m]) / ssU); break;
-          case 6: v = (float)((V1[m] - V2[m]) / ssV); break;
+          case 0: v = (float)(zb[m] - zb[nd]) / zref; break;
+          case 1: v = (float)fmax(S1[m] - zb[m], 0.0) / href; break;
+          case 2: v = (float)U1[m] / uref; break;
+          case 3: v = (float)V1[m] / uref; break;
+          case 4: v = (float)(S1[m] - S2[m]) / ssS; break;
+          case 5: v = (float)(U1[m] - U2[m]) / ssU; break;
+          case 6: v = (float)(V1[m] - V2[m]) / ssV; break;
           default: v = dist[(size_t)nd * K + s]; break;
         }
       }

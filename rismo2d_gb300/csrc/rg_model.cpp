@@ -148,6 +148,8 @@ struct rg_sim {
   std::vector<unsigned> ib_kind; // init_bcon work arrays (line nodes only are touched)
   std::vector<char> ib_has, ib_mark;
   std::vector<double> ib_vU, ib_vS;
+  // page-locked host state (cudaHostRegister), unregistered on destroy
+  std::vector<void*> pinned;
   // host wall time per stage of rg_sim_step (rg_sim_stage_ms)
   double stage_ms[RG_SIM_NSTAGE] = {};
   int stage_cur = -1;
@@ -897,6 +899,12 @@ rg_status rg_sim_create(const rg_deck* d, int precision, int device, rg_sim** ou
   if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
   st = rg_set_friction(s->ctx, s->en_n.data(), s->en_af.data());
   if (st != RG_OK) return sfail(s, st, rg_last_error(s->ctx));
+  // page-lock the node arrays the Newton loop moves between host and device (they keep their size)
+  for (std::vector<double>* v : {&s->U, &s->V, &s->S, &s->dUdt, &s->dVdt, &s->dSdt, &s->z, &s->cf, &s->bcU})
+    if (cudaHostRegister(v->data(), v->size() * sizeof(double), cudaHostRegisterDefault) == cudaSuccess)
+      s->pinned.push_back(v->data());
+    else
+      (void)cudaGetLastError();   // stays pageable: slower copies, same results
   return RG_OK;
 }
 
@@ -904,6 +912,7 @@ rg_ctx* rg_sim_context(rg_sim* s) { return s ? s->ctx : nullptr; }
 
 rg_status rg_sim_destroy(rg_sim* s) {
   if (!s) return RG_OK;
+  for (void* p : s->pinned) cudaHostUnregister(p);
   if (s->ctx) rg_destroy(s->ctx);
   delete s;
   return RG_OK;
