@@ -514,6 +514,7 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       TRY(c->EK64.alloc(nk));
     }
     TRY(c->EF.alloc((size_t)std::max<long long>(nasm, 1) * RG_EQ));
+    c->geo_valid = false;
   }
 
   // ILU(0) schedule: L positions sorted by column; split L/U operands
@@ -1010,6 +1011,7 @@ rg_status rg_set_elements(rg_ctx* c, int ne, const int* elem_nodes, const int* e
   }
   TRY(cudaSetDevice(c->device));
   c->ne = ne;
+  c->geo_valid = false;
   TRY(upload(c, c->enodes, elem_nodes, 6 * (size_t)ne));
   TRY(upload(c, c->ennd, elem_nnd, ne));
   TRY(upload(c, c->eflag, elem_flag, ne));

@@ -103,6 +103,7 @@ struct AsmArgs {
   const int* bnd;    // positions in elems of the boundary line elements
   int bcount;
   double g, hmin, vk, rUV, rH;
+  const double* geo;   // k_geometry output, per element of the list
 };
 
 // block-coefficient slots per Gauss point
@@ -119,6 +120,62 @@ enum {
   C_SH0, C_SHX, C_SHY,                   // H-derivative of continuity
   C_N
 };
+
+// Mesh geometry of the region triangles in the assembly lists, per Gauss
+// point: the integration weight detJ*w and the x/y derivatives of the P2 and
+// P1 shape functions (Jacobian transform of CoefsUVS2D.cpp:365-460).  It
+// depends on the node coordinates only, so it is computed once per element
+// list instead of once per Newton iteration; the arithmetic is the element
+// kernel's own.
+constexpr int GEO_PER_GP = 19;                  // w, dndx[6], dndy[6], dmdx[3], dmdy[3]
+constexpr int GEO_PER_ELEM = 7 * GEO_PER_GP;
+
+template <class KT>
+__global__ void k_geometry(AsmArgs a, double* __restrict__ geo) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < a.count * 7; t += gridDim.x * blockDim.x) {
+    const int g = t % 7;
+    const int e = a.elems[a.reg[t / 7]];
+    const int* nd = a.enodes + 6 * e;
+    double* o = geo + (size_t)e * GEO_PER_ELEM + g * GEO_PER_GP;
+    double x[6], y[6];
+    x[0] = 0.0;
+    y[0] = 0.0;
+    for (int i = 1; i < 6; i++) {
+      x[i] = a.x[nd[i]] - a.x[nd[0]];
+      y[i] = a.y[nd[i]] - a.y[nd[0]];
+    }
+    double j00 = 0, j01 = 0, j10 = 0, j11 = 0;
+    for (int k = 0; k < 6; k++) {
+      j00 += cS.dnx[g][k] * x[k];
+      j01 += cS.dnx[g][k] * y[k];
+      j10 += cS.dny[g][k] * x[k];
+      j11 += cS.dny[g][k] * y[k];
+    }
+    double detj = j00 * j11 - j01 * j10;
+    double t00, t01, t10, t11;
+    if constexpr (sizeof(KT) == 4) {   // mixed: one FP64 division instead of four
+      const double idet = 1.0 / detj;
+      t00 = j11 * idet, t01 = -j01 * idet, t10 = -j10 * idet, t11 = j00 * idet;
+    } else {
+      t00 = j11 / detj, t01 = -j01 / detj, t10 = -j10 / detj, t11 = j00 / detj;
+    }
+    o[0] = detj * cS.w[g];
+    double dndx[6], dndy[6], dmdx[3], dmdy[3];
+    for (int j = 0; j < 6; j++) {
+      dndx[j] = t00 * cS.dnx[g][j] + t01 * cS.dny[g][j];
+      dndy[j] = t10 * cS.dnx[g][j] + t11 * cS.dny[g][j];
+      o[1 + j] = dndx[j];
+      o[7 + j] = dndy[j];
+    }
+    const double dLx[3] = {-1.0, 1.0, 0.0}, dLy[3] = {-1.0, 0.0, 1.0};
+    for (int j = 0; j < 3; j++) {
+      dmdx[j] = t00 * dLx[j] + t01 * dLy[j];
+      dmdy[j] = t10 * dLx[j] + t11 * dLy[j];
+      o[13 + j] = dmdx[j];
+      o[16 + j] = dmdy[j];
+    }
+  }
+}
 
 // Jacobian block coefficients of one Gauss point (CoefsUVS2D.cpp:749-1059),
 // evaluated in R: FP64 for the FP64 Jacobian, FP32 for the FP32 one
@@ -340,42 +397,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_element(AsmArgs a, KT* __restric
       const int g = lane % 7;
       GpData<KT>& d = s.el[lane / 7];
       const int e = a.elems[a.reg[base + lane / 7]];
-      double x[6], y[6];
-      x[0] = 0.0;
-      y[0] = 0.0;
-      for (int i = 1; i < 6; i++) {
-        x[i] = d.nd[8][i] - d.nd[8][0];
-        y[i] = d.nd[9][i] - d.nd[9][0];
-      }
-      double j00 = 0, j01 = 0, j10 = 0, j11 = 0;
-      for (int k = 0; k < 6; k++) {
-        j00 += cS.dnx[g][k] * x[k];
-        j01 += cS.dnx[g][k] * y[k];
-        j10 += cS.dny[g][k] * x[k];
-        j11 += cS.dny[g][k] * y[k];
-      }
-      double detj = j00 * j11 - j01 * j10;
-      double t00, t01, t10, t11;
-      if constexpr (sizeof(KT) == 4) {   // mixed: one FP64 division instead of four
-        const double idet = 1.0 / detj;
-        t00 = j11 * idet, t01 = -j01 * idet, t10 = -j10 * idet, t11 = j00 * idet;
-      } else {
-        t00 = j11 / detj, t01 = -j01 / detj, t10 = -j10 / detj, t11 = j00 / detj;
-      }
-      double w = detj * cS.w[g];
+      // mesh geometry of this Gauss point (k_geometry)
+      const double* gp = a.geo + (size_t)e * GEO_PER_ELEM + g * GEO_PER_GP;
+      const double w = gp[0];
       double dndx[6], dndy[6], dmdx[3], dmdy[3];
       for (int j = 0; j < 6; j++) {
-        dndx[j] = t00 * cS.dnx[g][j] + t01 * cS.dny[g][j];
-        dndy[j] = t10 * cS.dnx[g][j] + t11 * cS.dny[g][j];
+        dndx[j] = gp[1 + j];
+        dndy[j] = gp[7 + j];
         d.dndx[g][j] = dndx[j];
         d.dndy[g][j] = dndy[j];
         d.kdndx[g][j] = (KT)dndx[j];
         d.kdndy[g][j] = (KT)dndy[j];
       }
-      const double dLx[3] = {-1.0, 1.0, 0.0}, dLy[3] = {-1.0, 0.0, 1.0};
       for (int j = 0; j < 3; j++) {
-        dmdx[j] = t00 * dLx[j] + t01 * dLy[j];
-        dmdy[j] = t10 * dLx[j] + t11 * dLy[j];
+        dmdx[j] = gp[13 + j];
+        dmdy[j] = gp[16 + j];
         d.dmdx[g][j] = dmdx[j];
         d.dmdy[g][j] = dmdy[j];
         d.kdmdx[g][j] = (KT)dmdx[j];
@@ -661,12 +697,14 @@ __global__ void k_asm_gather(long long nnz, const long long* __restrict__ gptr, 
   }
 }
 
+__global__ void k_pow_third(double h, double* out) { *out = pow(h, 0.333333); }
+
 // nodal Manning friction, gathered per node over its region triangles in
 // element order (DoFriction.cpp:87-206)
 __global__ void k_friction(int np, const int* __restrict__ nptr, const int* __restrict__ nel,
                            const double* __restrict__ elem_n, const double* __restrict__ elem_af,
                            const double* __restrict__ S, const double* __restrict__ z, double hmin, double g,
-                           double* __restrict__ cf) {
+                           const double* __restrict__ phmin, double* __restrict__ cf) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= np) return;
   int b = nptr[k], e = nptr[k + 1];
@@ -675,8 +713,8 @@ __global__ void k_friction(int np, const int* __restrict__ nptr, const int* __re
     return;
   }
   double h = S[k] - z[k];
-  if (h < hmin) h = hmin;
-  double ph = pow(h, 0.333333);
+  // depth clipped to hmin (every dry node): the same pow, evaluated once per context
+  const double ph = (h <= hmin) ? *phmin : pow(h, 0.333333);
   double acc = 0.0;
   for (int q = b; q < e; q++) {
     int el = nel[q];
@@ -715,6 +753,19 @@ cudaError_t launch_assemble(rg_ctx* c) {
   a.count = c->n_asm_reg;
   a.bnd = c->asm_bnd.p;
   a.bcount = c->n_asm_bnd;
+  if (!c->geo_valid) {
+    cudaError_t e = c->geo.alloc((size_t)std::max(c->ne, 1) * GEO_PER_ELEM);
+    if (e != cudaSuccess) return e;
+    if (a.count > 0) {
+      const int gblocks = std::min((a.count * 7 + 127) / 128, c->num_sms * 8);
+      if (c->prec == RG_PREC_MIXED)
+        k_geometry<float><<<gblocks, 128, 0, rg_counted(c)>>>(a, c->geo.p);
+      else
+        k_geometry<double><<<gblocks, 128, 0, rg_counted(c)>>>(a, c->geo.p);
+    }
+    c->geo_valid = true;
+  }
+  a.geo = c->geo.p;
   constexpr int EPW = 4;
   const int items = (a.count + EPW - 1) / EPW + a.bcount;
   const long long ntot = (long long)c->nnz + c->neq;
@@ -747,7 +798,13 @@ cudaError_t launch_assemble(rg_ctx* c) {
 
 cudaError_t launch_friction(rg_ctx* c) {
   int np = c->np;
+  if (c->fr_phmin_h != c->hmin) {
+    cudaError_t e = c->fr_phmin.alloc(1);
+    if (e != cudaSuccess) return e;
+    k_pow_third<<<1, 1, 0, rg_counted(c)>>>(c->hmin, c->fr_phmin.p);
+    c->fr_phmin_h = c->hmin;
+  }
   k_friction<<<(np + 255) / 256, 256, 0, rg_counted(c)>>>(np, c->fr_ptr.p, c->fr_el.p, c->elem_n.p, c->elem_af.p,
-                                                   c->S.p, c->z.p, c->hmin, c->g, c->cf.p);
+                                                   c->S.p, c->z.p, c->hmin, c->g, c->fr_phmin.p, c->cf.p);
   return cudaGetLastError();
 }

@@ -161,6 +161,8 @@ struct rg_ctx {
   DBuf<int> gat_src;                 // position * RG_EQ*RG_EQ + r * RG_EQ + c
   DBuf<int> grow_src;                // position * RG_EQ + r
   DBuf<double> EK64, EF;             // element matrices (FP64 Jacobian), element residuals
+  DBuf<double> geo;                  // per region triangle: Gauss-point weights and shape derivatives
+  bool geo_valid = false;            // geo matches the current element lists
   DBuf<float> EK32;                  // element matrices (FP32 Jacobian)
 
   // values
@@ -194,6 +196,8 @@ struct rg_ctx {
   int np_model = 0, ne_region = 0;
   DBuf<double> elem_n, elem_af;  // friction: Manning n, area factor per region triangle
   DBuf<int> fr_ptr, fr_el;       // node -> region triangles (element order)
+  DBuf<double> fr_phmin;         // hmin^0.333333 as the friction kernel's pow gives it
+  double fr_phmin_h = -1.0;      // the hmin it was computed for
 
   // timings
   cudaEvent_t ev[16];
