@@ -37,7 +37,7 @@ def _compile(src: str) -> str:
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     if src.endswith(".cpp"):
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I/usr/local/cuda/include", "-c"]
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-I/usr/local/cuda/include", "-c"]
     else:
         cmd = [_nvcc()] + ARCH + FLAGS + ["-c"]
     subprocess.check_call(cmd + [os.path.join(CSRC, src), "-o", obj])
@@ -53,7 +53,7 @@ def build(force: bool = False) -> str:
         objs = list(ex.map(_compile, SOURCES))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp"
-        subprocess.check_call([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        subprocess.check_call([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB)
     return LIB
 

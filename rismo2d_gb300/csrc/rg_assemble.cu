@@ -488,9 +488,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_element(AsmArgs a, KT* __restric
       GpData<KT>& d = s.el[j];
       bool have_area = false;
 
-      // 3. trial vectors: 7 GP x 9 blocks x 6 columns (t, tx, ty)
-      for (int idx = lane; idx < 7 * 9 * 6; idx += 32) {
-        const int g = idx / 54, r = idx % 54, b = r / 6, k = r % 6;
+      // 3. trial vectors: 7 GP x 9 blocks x 6 columns (t, tx, ty), one block per
+      // pass so that the block switch is warp-uniform
+#pragma unroll 1
+      for (int b = 0; b < 9; b++)
+      for (int idx = lane; idx < 7 * 6; idx += 32) {
+        const int g = idx / 6, k = idx % 6;
         const KT* c = d.coef[g];
         const KT nk = shape_n<KT>(g, k), xk = d.kdndx[g][k], yk = d.kdndy[g][k];
         KT t = 0, tx = 0, ty = 0;

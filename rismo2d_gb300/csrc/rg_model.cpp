@@ -26,11 +26,15 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -94,6 +98,81 @@ double interp_hydro(const LineBc& b, double t, double* Sspec) {
   return Q;
 }
 
+// A fixed set of host threads for the data-parallel passes of the host model
+// (dry/rewet, connectivity counts).  run(n, fn) calls fn(begin, end, t) on
+// contiguous slices of [0, n), slice t on thread t, and returns when all are
+// done; every pass it runs either writes per-item results or combines into
+// shared words with commutative atomic operations, so results do not depend
+// on the thread count.
+class HostPool {
+ public:
+  explicit HostPool(int nthreads) : nt_(std::max(1, nthreads)) {
+    for (int t = 1; t < nt_; t++) workers_.emplace_back([this, t] { worker(t); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread& w : workers_) w.join();
+  }
+  template <class F>
+  void run(long long n, F&& fn) {
+    if (nt_ == 1 || n < 8192) {
+      fn(0ll, n, 0);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      task_ = [&fn, n, this](int t) { fn(n * t / nt_, n * (t + 1) / nt_, t); };
+      pending_ = nt_ - 1;
+      gen_++;
+    }
+    cv_.notify_all();
+    task_(0);
+    std::unique_lock<std::mutex> lk(m_);
+    done_.wait(lk, [this] { return pending_ == 0; });
+  }
+  int threads() const { return nt_; }
+
+ private:
+  void worker(int t) {
+    long long seen = 0;
+    for (;;) {
+      std::function<void(int)> task;
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+        task = task_;
+      }
+      task(t);
+      std::lock_guard<std::mutex> lk(m_);
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  int nt_;
+  std::vector<std::thread> workers_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  std::function<void(int)> task_;
+  long long gen_ = 0;
+  int pending_ = 0;
+  bool stop_ = false;
+};
+
+int host_threads() {
+  const char* e = getenv("RG_HOST_THREADS");
+  if (e && atoi(e) > 0) return std::min(atoi(e), 64);
+  const unsigned h = std::thread::hardware_concurrency();
+  return (int)std::min(16u, std::max(1u, h));
+}
+
+inline void atomic_or(unsigned* p, unsigned v) { __atomic_fetch_or(p, v, __ATOMIC_RELAXED); }
+inline void atomic_and(unsigned* p, unsigned v) { __atomic_fetch_and(p, v, __ATOMIC_RELAXED); }
+
 }  // namespace
 
 struct rg_sim {
@@ -150,6 +229,12 @@ struct rg_sim {
   std::vector<double> ib_vU, ib_vS;
   // page-locked host state (cudaHostRegister), unregistered on destroy
   std::vector<void*> pinned;
+  // host threads of the dry/rewet and connectivity passes; dry/rewet work arrays
+  std::unique_ptr<HostPool> pool;
+  std::vector<int> mid_owner;    // mid-side node -> first triangle that has it
+  std::vector<char> dw_nmark, dw_emark;
+  std::vector<std::vector<int>> dw_marsh;   // per slice: non-dry triangles with a marsh corner
+  std::vector<unsigned> dw_nflag0, dw_eflag0; // flags before the last dry/rewet pass
   // host wall time per stage of rg_sim_step (rg_sim_stage_ms)
   double stage_ms[RG_SIM_NSTAGE] = {};
   int stage_cur = -1;
@@ -173,11 +258,14 @@ static rg_status sfail(rg_sim* s, rg_status st, const std::string& m) {
 // ---- MODEL::Initialize and helpers ----------------------------------------
 
 static void connection(rg_sim* s, unsigned dry) {
-  std::fill(s->noel.begin(), s->noel.end(), 0);
-  for (int e = 0; e < s->ne; e++) {
-    if (dry && (s->eflag[e] & dry)) continue;
-    for (int i = 0; i < 6; i++) s->noel[s->en[6 * e + i]]++;
-  }
+  int* noel = s->noel.data();
+  s->pool->run(s->np, [&](long long b, long long e, int) { std::fill(noel + b, noel + e, 0); });
+  s->pool->run(s->ne, [&](long long b, long long e, int) {
+    for (long long k = b; k < e; k++) {
+      if (dry && (s->eflag[k] & dry)) continue;
+      for (int i = 0; i < 6; i++) __atomic_fetch_add(&noel[s->en[6 * k + i]], 1, __ATOMIC_RELAXED);
+    }
+  });
 }
 
 static void boundary(rg_sim* s) {
@@ -605,87 +693,130 @@ static rg_status set_eqno(rg_sim* s) {
 // ---- GRID::DryRewet, method 2 -----------------------------------------------
 
 static void dry_rewet(rg_sim* s, int* dried, int* wetted) {
+  // GRID::DryRewet method 2 (DryRewet.cpp:696-990), the passes of the
+  // reference in its order; node and element passes run on the host threads
+  // (per-item writes, commutative flag updates), the marsh-corner water
+  // levels -- which read levels set earlier in the same pass -- in element order
   const double dryLimit = s->p.dry_limit, rewetLimit = s->p.rewet_limit;
   const int countDown = s->p.countdown;
-  std::vector<char> nmark(s->np), emark(s->ne);
-  for (int n = 0; n < s->np; n++) {
-    nmark[n] = (s->nflag[n] & N_DRY) != 0;
-    s->nflag[n] &= ~N_MARSH;
-    double H = s->S[n] - s->zor[n];
-    if (H < dryLimit) {
-      s->nflag[n] |= N_DRY;
-      s->countdown[n] = countDown;
-    } else {
-      if (s->countdown[n] > 0)
-        s->countdown[n]--;
-      else
-        s->nflag[n] &= ~N_DRY;
-    }
-    s->z[n] = s->zor[n];
-  }
-  for (int e = 0; e < s->ne; e++) {
-    emark[e] = (s->eflag[e] & E_DRY) != 0;
-    s->eflag[e] &= ~(E_DRY | E_MARSH);
-    const int* nd = &s->en[6 * e];
-    int ndry = 0;
-    for (int i = 0; i < 3; i++)
-      if (s->nflag[nd[i]] & N_DRY) ndry++;
-    if (ndry == 3) {
-      s->eflag[e] |= E_DRY;
-    } else if (ndry) {
-      s->eflag[e] |= E_MARSH;
-      for (int i = 0; i < 3; i++)
-        if (s->nflag[nd[i]] & N_DRY) s->nflag[nd[i]] |= N_MARSH;
-    }
-  }
-  for (int n = 0; n < s->np; n++) s->nflag[n] |= N_DRY;
-  for (int e = 0; e < s->ne; e++) {
-    if (s->eflag[e] & E_DRY) continue;
-    const int* nd = &s->en[6 * e];
-    for (int i = 0; i < 6; i++) s->nflag[nd[i]] &= ~N_DRY;
-    for (int i = 0; i < 3; i++) {
-      const int ni = nd[i];
-      if (!(s->nflag[ni] & N_MARSH)) continue;
-      if (nmark[ni] || s->firstDryRew) {
-        int j = (i + 1) % 3, k = (i + 2) % 3;
-        double Si;
-        bool mj = (s->nflag[nd[j]] & N_MARSH) != 0, mk = (s->nflag[nd[k]] & N_MARSH) != 0;
-        if (!mj && !mk)
-          Si = (s->S[nd[j]] + s->S[nd[k]]) / 2.0;
-        else if (!mj)
-          Si = s->S[nd[j]];
-        else if (!mk)
-          Si = s->S[nd[k]];
-        else
-          Si = s->S[nd[(i + 2) % 3]];   // all corners marsh cannot happen for a marsh element
-        s->S[ni] = Si;
-        if (s->S[ni] > s->zor[ni] + rewetLimit) s->S[ni] = s->zor[ni] + rewetLimit;
-        if (s->S[ni] < s->zor[ni] + dryLimit) s->z[ni] = s->S[ni] - dryLimit;
+  const int np = s->np, ne = s->ne;
+  std::vector<char>& nmark = s->dw_nmark;
+  std::vector<char>& emark = s->dw_emark;
+  nmark.resize(np);
+  emark.resize(ne);
+  unsigned* nflag = s->nflag.data();
+  unsigned* eflag = s->eflag.data();
+  const int* en = s->en.data();
+  double* S = s->S.data();
+  double* z = s->z.data();
+  const double* zor = s->zor.data();
+  HostPool& pool = *s->pool;
+  pool.run(np, [&](long long b, long long e, int) {
+    for (long long n = b; n < e; n++) {
+      nmark[n] = (nflag[n] & N_DRY) != 0;
+      nflag[n] &= ~N_MARSH;
+      double H = S[n] - zor[n];
+      if (H < dryLimit) {
+        nflag[n] |= N_DRY;
+        s->countdown[n] = countDown;
       } else {
-        if (s->S[ni] < s->zor[ni] + dryLimit) s->z[ni] = s->S[ni] - dryLimit;
+        if (s->countdown[n] > 0)
+          s->countdown[n]--;
+        else
+          nflag[n] &= ~N_DRY;
+      }
+      z[n] = zor[n];
+    }
+  });
+  pool.run(ne, [&](long long b, long long ee, int) {
+    for (long long e = b; e < ee; e++) {
+      emark[e] = (eflag[e] & E_DRY) != 0;
+      eflag[e] &= ~(E_DRY | E_MARSH);
+      const int* nd = &en[6 * e];
+      int ndry = 0;
+      for (int i = 0; i < 3; i++)
+        if (nflag[nd[i]] & N_DRY) ndry++;
+      if (ndry == 3) {
+        eflag[e] |= E_DRY;
+      } else if (ndry) {
+        eflag[e] |= E_MARSH;
+        for (int i = 0; i < 3; i++)
+          if (nflag[nd[i]] & N_DRY) atomic_or(&nflag[nd[i]], N_MARSH);
       }
     }
-  }
-  for (int e = 0; e < s->ne; e++) {
-    const int* nd = &s->en[6 * e];
-    for (int i = 3; i < 6; i++) {
-      int l = nd[i - 3], r = nd[(i - 2) % 3];
-      s->S[nd[i]] = 0.5 * (s->S[l] + s->S[r]);
-      s->z[nd[i]] = 0.5 * (s->z[l] + s->z[r]);
-      if ((s->eflag[e] & E_MARSH) && s->z[nd[i]] + dryLimit / 10.0 < s->zor[nd[i]]) s->nflag[nd[i]] |= N_MARSH;
+  });
+  pool.run(np, [&](long long b, long long e, int) {
+    for (long long n = b; n < e; n++) nflag[n] |= N_DRY;
+  });
+  // wet triangles clear kDry on their nodes; the ones with a marsh corner are listed in order
+  const int nt = pool.threads();
+  s->dw_marsh.resize(nt);
+  for (auto& l : s->dw_marsh) l.clear();
+  pool.run(ne, [&](long long b, long long ee, int t) {
+    std::vector<int>& lst = s->dw_marsh[t];
+    for (long long e = b; e < ee; e++) {
+      if (eflag[e] & E_DRY) continue;
+      const int* nd = &en[6 * e];
+      for (int i = 0; i < 6; i++) atomic_and(&nflag[nd[i]], ~(unsigned)N_DRY);
+      if ((nflag[nd[0]] | nflag[nd[1]] | nflag[nd[2]]) & N_MARSH) lst.push_back((int)e);
     }
-  }
-  for (int n = 0; n < s->np; n++) {
-    if (s->nflag[n] & N_DRY) {
-      s->U[n] = s->V[n] = 0.0;
-      s->S[n] = s->z[n] = s->zor[n];
-      s->dUdt[n] = s->dVdt[n] = s->dSdt[n] = 0.0;
+  });
+  for (const std::vector<int>& lst : s->dw_marsh)
+    for (int e : lst) {
+      const int* nd = &en[6 * e];
+      for (int i = 0; i < 3; i++) {
+        const int ni = nd[i];
+        if (!(nflag[ni] & N_MARSH)) continue;
+        if (nmark[ni] || s->firstDryRew) {
+          int j = (i + 1) % 3, k = (i + 2) % 3;
+          double Si;
+          bool mj = (nflag[nd[j]] & N_MARSH) != 0, mk = (nflag[nd[k]] & N_MARSH) != 0;
+          if (!mj && !mk)
+            Si = (S[nd[j]] + S[nd[k]]) / 2.0;
+          else if (!mj)
+            Si = S[nd[j]];
+          else if (!mk)
+            Si = S[nd[k]];
+          else
+            Si = S[nd[(i + 2) % 3]];   // all corners marsh cannot happen for a marsh element
+          S[ni] = Si;
+          if (S[ni] > zor[ni] + rewetLimit) S[ni] = zor[ni] + rewetLimit;
+          if (S[ni] < zor[ni] + dryLimit) z[ni] = S[ni] - dryLimit;
+        } else {
+          if (S[ni] < zor[ni] + dryLimit) z[ni] = S[ni] - dryLimit;
+        }
+      }
     }
-  }
+  // mid-side levels from the corners: every triangle of a mid-side gives the same
+  // value, the first one writes it; any marsh triangle may flag it
+  pool.run(ne, [&](long long b, long long ee, int) {
+    for (long long e = b; e < ee; e++) {
+      const int* nd = &en[6 * e];
+      for (int i = 3; i < 6; i++) {
+        int l = nd[i - 3], r = nd[(i - 2) % 3];
+        const double Sm = 0.5 * (S[l] + S[r]);
+        const double zm = 0.5 * (z[l] + z[r]);
+        if (s->mid_owner[nd[i]] == e) {
+          S[nd[i]] = Sm;
+          z[nd[i]] = zm;
+        }
+        if ((eflag[e] & E_MARSH) && zm + dryLimit / 10.0 < zor[nd[i]]) atomic_or(&nflag[nd[i]], N_MARSH);
+      }
+    }
+  });
+  pool.run(np, [&](long long b, long long e, int) {
+    for (long long n = b; n < e; n++) {
+      if (nflag[n] & N_DRY) {
+        s->U[n] = s->V[n] = 0.0;
+        S[n] = z[n] = zor[n];
+        s->dUdt[n] = s->dVdt[n] = s->dSdt[n] = 0.0;
+      }
+    }
+  });
   int d = 0, w = 0;
-  for (int e = 0; e < s->ne; e++) {
-    if ((s->eflag[e] & E_DRY) && !emark[e]) d++;
-    if (!(s->eflag[e] & E_DRY) && emark[e]) w++;
+  for (int e = 0; e < ne; e++) {
+    if ((eflag[e] & E_DRY) && !emark[e]) d++;
+    if (!(eflag[e] & E_DRY) && emark[e]) w++;
   }
   *dried = d;
   *wetted = w;
@@ -761,7 +892,9 @@ static void slip_flow(rg_sim* s) {
 }
 
 static void do_dry_rewet(rg_sim* s, int* del, int* wel) {
-  s->bc_valid = false;
+  // the boundary set-up stays valid when the pass leaves every node and element flag as it was
+  s->dw_nflag0 = s->nflag;
+  s->dw_eflag0 = s->eflag;
   connection(s, 0);
   *del = *wel = 0;
   if (s->p.dryrew_method == 2) dry_rewet(s, del, wel);
@@ -773,6 +906,7 @@ static void do_dry_rewet(rg_sim* s, int* del, int* wel) {
   } else {
     connection(s, E_DRY);
   }
+  if (*del + *wel || s->nflag != s->dw_nflag0 || s->eflag != s->dw_eflag0) s->bc_valid = false;
   s->firstDryRew = false;
 }
 
@@ -807,6 +941,11 @@ rg_status rg_sim_create(const rg_deck* d, int precision, int device, rg_sim** ou
   }
   s->z = s->zor;
   s->en.assign(d->elem_nodes, d->elem_nodes + 6 * (size_t)d->ne);
+  s->pool.reset(new HostPool(host_threads()));
+  s->mid_owner.assign(d->np, -1);
+  for (int e = 0; e < d->ne; e++)
+    for (int i = 3; i < 6; i++)
+      if (s->mid_owner[s->en[6 * e + i]] < 0) s->mid_owner[s->en[6 * e + i]] = e;
   s->en_n.resize(d->ne);
   s->en_vt.resize(d->ne);
   for (int e = 0; e < d->ne; e++) {
