@@ -244,7 +244,7 @@ struct WarpSmem {
 // element by element with all lanes.  Work items from nregw on are boundary
 // line elements, one per warp: lane 0 integrates, all lanes store.
 template <class KT, int WARPS, int EPW>
-__global__ void __launch_bounds__(WARPS * 32) k_element(AsmArgs a, KT* __restrict__ EK, double* __restrict__ EF) {
+__global__ void __launch_bounds__(WARPS * 32, 6) k_element(AsmArgs a, KT* __restrict__ EK, double* __restrict__ EF) {
   __shared__ WarpSmem<KT, EPW> smem[WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
