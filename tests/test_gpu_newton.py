@@ -60,3 +60,25 @@ def test_unsteady_meander_three_steps(prec):
         assert np.array_equal(got["flag"] & DRY, g[f"step{i}_flag"] & DRY), f"dry flags differ after step {i}"
         _compare(got, g[f"step{i}_U"], g[f"step{i}_V"], g[f"step{i}_S"], g[f"step{i}_z"], TOL[prec])
     sim.close()
+
+
+@pytest.mark.parametrize("name", list(CHANNELS))
+@pytest.mark.parametrize("prec", [0, 2])
+@pytest.mark.parametrize("forcing,reuse", [(0.5, 64), (0.1, 0), (0.0, 1000)])
+def test_steady_channel_inexact_newton(name, prec, forcing, reuse):
+    """Inexact Newton (BiCGStab to the forcing term) and reused ILU(0) factors
+    change only the path: the step still reaches ||B||/||B_0|| <= 1e-8 and the
+    reference's converged state within the acceptance tolerance."""
+    g = golden_io.load(name)
+    mesh = meshgen.channel(**CHANNELS[name])
+    sim = Simulation(mesh, Params(max_newton=200), precision=prec)
+    sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+    rep = sim.step(0.0, 3600.0, steady=True, criterion=RG_CRIT_RESIDUAL, residual_tol=1e-8,
+                   linear_forcing=forcing, ilu_reuse=reuse)
+    assert rep["converged"] and rep["residual_ratio"] <= 1e-8
+    got = sim.get_state()
+    _compare(got, g["final_U"], g["final_V"], g["final_S"], g["final_z"], TOL[prec])
+    assert np.array_equal(got["flag"] & DRY, g["final_flag"] & DRY)
+    stages = sim.stage_ms()
+    assert stages["krylov"] > 0.0 and stages["assemble"] > 0.0
+    sim.close()
