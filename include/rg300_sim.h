@@ -90,8 +90,9 @@ typedef struct {
   double linear_forcing;
   /* 0: ILU(0) is factored in every Newton iteration (the reference).  n > 0:
    * the resident factors precondition up to n further Newton iterations (also
-   * across time steps) while the numbering is unchanged; a solve that misses
-   * its tolerance forces fresh factors.  No counterpart in the reference. */
+   * across time steps) while the numbering is unchanged; a solve with reused
+   * factors that misses its tolerance (or breaks down) is repeated at once
+   * with fresh factors.  No counterpart in the reference. */
   int    ilu_reuse;
 } rg_step_ctl;
 

@@ -1428,6 +1428,17 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     const double lin_tol = std::max(s->p.solver_maxdiff, ctl->linear_forcing);
     st = rg_bicgstab(s->ctx, s->p.solver_maxiter, lin_tol, nullptr, &its, nullptr);
     krylov_total += its;
+    if ((st == RG_NOT_CONVERGED || st == RG_ERR_NONFINITE) && s->factor_age > 0) {
+      // the factors of an earlier iteration did not do: factor this matrix and solve again
+      STAGE("factor", RG_STAGE_FACTOR);
+      st = rg_ilu0_factor(s->ctx, nullptr, nullptr);
+      if (st != RG_OK) return st;
+      s->factor_eqs = s->eqs_init;
+      s->factor_age = 0;
+      STAGE("bicgstab", RG_STAGE_KRYLOV);
+      st = rg_bicgstab(s->ctx, s->p.solver_maxiter, lin_tol, nullptr, &its, nullptr);
+      krylov_total += its;
+    }
     if (st != RG_OK && st != RG_NOT_CONVERGED) return st;
     if (st == RG_NOT_CONVERGED) {
       status_solve = RG_NOT_CONVERGED;

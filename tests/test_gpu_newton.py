@@ -67,15 +67,17 @@ def test_unsteady_meander_three_steps(prec):
 @pytest.mark.parametrize("forcing,reuse", [(0.5, 64), (0.1, 0), (0.0, 1000)])
 def test_steady_channel_inexact_newton(name, prec, forcing, reuse):
     """Inexact Newton (BiCGStab to the forcing term) and reused ILU(0) factors
-    change only the path: the step still reaches ||B||/||B_0|| <= 1e-8 and the
+    change only the path to the solution.  From the cold start of a steady run
+    ||B_0|| is large, so the step is iterated to ||B||/||B_0|| <= 1e-11 (the
+    final state then no longer depends on the path) and must reach the
     reference's converged state within the acceptance tolerance."""
     g = golden_io.load(name)
     mesh = meshgen.channel(**CHANNELS[name])
-    sim = Simulation(mesh, Params(max_newton=200), precision=prec)
+    sim = Simulation(mesh, Params(max_newton=400), precision=prec)
     sim.set_state(mesh.U0, mesh.V0, mesh.S0)
-    rep = sim.step(0.0, 3600.0, steady=True, criterion=RG_CRIT_RESIDUAL, residual_tol=1e-8,
+    rep = sim.step(0.0, 3600.0, steady=True, criterion=RG_CRIT_RESIDUAL, residual_tol=1e-11,
                    linear_forcing=forcing, ilu_reuse=reuse)
-    assert rep["converged"] and rep["residual_ratio"] <= 1e-8
+    assert rep["converged"] and rep["residual_ratio"] <= 1e-11
     got = sim.get_state()
     _compare(got, g["final_U"], g["final_V"], g["final_S"], g["final_z"], TOL[prec])
     assert np.array_equal(got["flag"] & DRY, g["final_flag"] & DRY)
