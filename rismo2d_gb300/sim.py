@@ -86,7 +86,11 @@ class Simulation:
     """A mesh, its boundary conditions and the GPU state of one run."""
 
     def __init__(self, mesh, params: Params | None = None, hydrograph=None, precision: int = _lib.PREC_FP64,
-                 device: int = 0):
+                 device: int = 0, line_bcs=None):
+        """``line_bcs`` (optional): [(kind, line, rows)] with kind "QINLET" (rows [(Q, S)]),
+        "QTINLET" (rows [(t, Q, S)]) or "OUTLET" (rows [(S,)]) -- the $TM_LINE conditions
+        of a deck (deck.read_deck).  Without it: the inlet on line 1 (QINLET with the
+        mesh's Q, or QTINLET with ``hydrograph``) and the outlet level on line 2."""
         self.lib = _lib.load()
         self.lib.rg_sim_last_error.restype = C.c_char_p
         self.params = params or Params()
@@ -109,8 +113,23 @@ class Simulation:
         self._arr["segs"] = np.ascontiguousarray(np.asarray(segs, np.int32).reshape(-1))
         self._arr["lines"] = np.ascontiguousarray(lines, np.int32)
         bcs = []
-        S_in = m.meta.get("S_in", m.meta["S_out"])
-        if hydrograph is None:
+        if line_bcs is not None:
+            kinds = {"QINLET": RG_BC_QINLET, "QTINLET": RG_BC_QTINLET, "OUTLET": RG_BC_OUTLET}
+            for i, (kind, line, rows) in enumerate(line_bcs):
+                r = np.asarray(rows, np.float64).reshape(len(rows), -1)
+                if kind == "QTINLET":
+                    t, Q, S = r[:, 0], r[:, 1], r[:, 2]
+                elif kind == "QINLET":
+                    t, Q, S = np.zeros(1), r[:1, 0], r[:1, 1]
+                else:
+                    t, Q, S = np.zeros(1), np.zeros(1), r[:1, 0]
+                for nm, arr in (("t", t), ("Q", Q), ("S", S)):
+                    self._arr[f"bc{i}_{nm}"] = np.ascontiguousarray(arr, np.float64)
+                a_ = self._arr
+                bcs.append(LineBc(kinds[kind], int(line), len(a_[f"bc{i}_t"]), p(a_[f"bc{i}_t"]), p(a_[f"bc{i}_Q"]),
+                                  p(a_[f"bc{i}_S"])))
+        elif hydrograph is None:
+            S_in = m.meta.get("S_in", m.meta["S_out"])
             self._arr["q_t"] = np.array([0.0])
             self._arr["q_Q"] = np.array([float(m.meta["Q"])])
             self._arr["q_S"] = np.array([float(S_in)])
@@ -122,8 +141,9 @@ class Simulation:
             self._arr["q_S"] = np.ascontiguousarray(h[:, 2])
             bcs.append(LineBc(RG_BC_QTINLET, 1, len(h), p(self._arr["q_t"]), p(self._arr["q_Q"]),
                               p(self._arr["q_S"])))
-        self._arr["o_S"] = np.array([float(m.meta["S_out"])])
-        bcs.append(LineBc(RG_BC_OUTLET, 2, 1, None, None, p(self._arr["o_S"])))
+        if line_bcs is None:
+            self._arr["o_S"] = np.array([float(m.meta["S_out"])])
+            bcs.append(LineBc(RG_BC_OUTLET, 2, 1, None, None, p(self._arr["o_S"])))
         self._bcs = (LineBc * len(bcs))(*bcs)
         pp = self.params
         dp = DeckParams(pp.g, pp.vk, pp.dry_limit, pp.rewet_limit, pp.dryrew_method, pp.dryrew_freq, pp.countdown,
