@@ -331,6 +331,13 @@ def read_deck(main_path: str) -> DeckRun:
             steady = int(tok[0]) != 0
         elif key == "TM_MAXITER":
             maxit = int(tok[0])
+        elif key == "TM_CYCLE":
+            # cycles of a time step (Timeint.cpp:2003-2019): only the Taylor-Hood flow
+            # cycle (kUVSCyc = 1, Project.h:102) is on this path; e.g. the element
+            # reordering cycle 95 (Compute.cpp:666-680) is not
+            cyc = [int(v) for v in " ".join(tok).replace(",", " ").split()]
+            if any(c != 1 for c in cyc):
+                raise ValueError(f"$TM_CYCLE {' '.join(map(str, cyc))}: only cycle 1 (UVS flow) is supported")
         elif key == "TM_LINE":
             kind, no = tok[0], int(tok[1])
             v = [float(a) for a in tok[2:]]
