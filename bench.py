@@ -282,7 +282,11 @@ def run_gpu(prec: int, warmup: int, steps: int, device: int, profile: bool, cloc
     if profile:
         sim.profile(False)
     # the network's launches per prediction: features + forward
+    mod = sim.model()
+    wet_tri = int(np.count_nonzero(np.asarray(mod["elem_nnd"]) == 6))
+    wet_nodes = int(np.count_nonzero((states[-1]["flag"] & 64) == 0)) if states else 0
     out = dict(dev_ms=dev_ms, e2e_ms=e2e_ms, wall_s=wall1 - wall0, reps=timed, warm_reps=reps, states=states,
+               wet_tri=wet_tri, wet_nodes=wet_nodes,
                stats=st1.tolist(), h2d=int(st1[12] - st0[12]) + pred_h2d, d2h=int(st1[13] - st0[13]) + pred_d2h,
                launches=int(st1[14] - st0[14]) + (2 * steps if net else 0), prof=prof, clocks=clk, stage=stage)
     sim.close()
@@ -412,6 +416,28 @@ def trsv_roofline(prof, neq: int, nnz: int, w: int, wx: int):
             "traffic": NCU_TRSV_TRAFFIC_BYTES, "algorithmic_bytes_per_launch": per_launch,
             "launches": launches, "avg_launch_ms": round(ms / launches, 4),
             "share_of_step_device_time": None}
+
+
+def class_rooflines(prof, neq: int, nnz: int, tri: int, nodes: int, w: int = 4, wx: int = 4):
+    """Achieved bandwidth of every profiled kernel class from the live event timing, with the
+    algorithmic bytes per launch of its formula: SpMV z(w+4) + 4(n+1) + 2n wx; ILU(0) apply
+    z(w+4) + 4(n+1) + 3n wx per L+U pair; factor 2zw + 4z + 4(n+1); assembly zw + 8n + 120N
+    + 24T + 900T (T wet triangles, N wet nodes).  The refinement residual's SpMV reads FP64
+    vectors, so the SpMV class figure is a lower bound."""
+    peak, kind = hbm_peak()
+    per_launch = {"spmv": nnz * (w + 4) + 4 * (neq + 1) + 2 * neq * wx,
+                  "trsv": (nnz * (w + 4) + 4 * (neq + 1) + 3 * neq * wx) / 2.0,
+                  "factor": 2 * nnz * w + 4 * nnz + 4 * (neq + 1),
+                  "assemble": nnz * w + 8 * neq + 120 * nodes + 24 * tri + 900 * tri}
+    out = {}
+    for cls, (launches, ms) in prof.items():
+        if cls not in per_launch or launches == 0 or ms <= 0:
+            continue
+        gbs = per_launch[cls] * launches / (ms / 1e3) / 1e9
+        out[cls] = {"launches": launches, "avg_launch_ms": round(ms / launches, 4),
+                    "algorithmic_bytes_per_launch": int(per_launch[cls]), "achieved_gbs": round(gbs, 2),
+                    "frac": round(gbs / peak, 5)}
+    return {"peak_gbs": peak, "peak_kind": kind, "classes": out}
 
 
 def main():
@@ -561,7 +587,10 @@ def main():
                         "api": "Simulation.step + get_state (host numpy state out)"},
                 "gpu_launches": mixed["launches"],
                 "device_ms_by_kernel_class": {kk: [v[0], round(v[1], 2)] for kk, v in mixed["prof"].items()},
-                "roofline": roof, "cpu_baseline": cpu}
+                "roofline": roof,
+                "roofline_by_kernel_class": class_rooflines(mixed["prof"], int(st[0]), int(st[1]), mixed["wet_tri"],
+                                                            mixed["wet_nodes"]),
+                "cpu_baseline": cpu}
         if args.max_newton:
             line["profiling_case"] = f"Newton capped at {args.max_newton} per step: not a benchmark result"
         print(json.dumps(line), flush=True)

@@ -747,10 +747,11 @@ __global__ void k_bicg_restart_fin(const double* partial, int nparts, KrylovScal
   }
 }
 // FP64 residual of the refinement loop: r = B - t; r32 = (float) r; partial ||r||^2
+// t == nullptr: X = 0, the residual is B itself
 __global__ void k_resid(int n, const double* B, const double* t, float* r32, double* partial) {
   double acc[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double r = B[i] - t[i];
+    double r = t ? B[i] - t[i] : B[i];
     r32[i] = (float)r;
     acc[0] += r * r;
   }
@@ -1067,8 +1068,8 @@ rg_status run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, doubl
   int total = 0;
   rg_status st = RG_NOT_CONVERGED;
   for (int refine = 0; refine < 12; refine++) {
-    spmv_t<double, float, double, 0>(c, c->A32.p, c->X.p, c->tt.p, nullptr, nbs, nullptr);
-    k_resid<<<nb, 256, 0, rg_counted(c)>>>(n, c->B.p, c->tt.p, c->f_b.p, c->partial.p);
+    if (refine > 0) spmv_t<double, float, double, 0>(c, c->A32.p, c->X.p, c->tt.p, nullptr, nbs, nullptr);
+    k_resid<<<nb, 256, 0, rg_counted(c)>>>(n, c->B.p, refine > 0 ? c->tt.p : nullptr, c->f_b.p, c->partial.p);
     k_fin_to<<<1, 256, 0, rg_counted(c)>>>(c->partial.p, nb, &c->ks.p->t2);
     c->d2h_bytes += sizeof(KrylovScalars);
     e = cudaMemcpyAsync(c->ks_host, c->ks.p, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, c->st);
