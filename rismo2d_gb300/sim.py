@@ -62,7 +62,7 @@ class StepReport(C.Structure):
 
 @dataclasses.dataclass
 class Params:
-    """Deck parameters; defaults are the survey decks' $RELAX/$DRYREW/$SOLVER lines."""
+    """Deck parameters; defaults are the $RELAX/$DRYREW/$SOLVER lines deck.write_deck writes."""
     g: float = 9.81
     vk: float = 1.78e-6 / (1.0 + 0.0337 * 10.0 + 0.00022 * 100.0)   # Project.cpp:110, 10 degC
     dry_limit: float = 0.01
