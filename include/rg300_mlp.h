@@ -14,8 +14,9 @@
  *
  * Network: 128 inputs (15 stencil nodes x 8 features + discharge ratios),
  * three hidden layers of 128 with GELU, 3 outputs; BF16 weights and
- * activations, FP32 accumulation; forward on the tensor cores (mma.sync
- * bf16), backward and Adam in FP32.  Trained on the GPU from time-level
+ * activations, FP32 accumulation; forward and the backward products of the
+ * 128-wide layers on the tensor cores (mma.sync bf16, the upstream gradient
+ * rounded to bf16), the 3-output layer's backward and Adam in FP32.  Trained on the GPU from time-level
  * triples a caller collects from the plain solver.
  *
  * All arrays are HOST memory; node arrays are indexed like the rg_sim node

@@ -1,6 +1,7 @@
 // Learned Newton warm start (include/rg300_mlp.h): stencil features, the
-// network's forward pass on the tensor cores (mma.sync m16n8k16, bf16 inputs,
-// fp32 accumulation), its backward pass and Adam in fp32.
+// network's forward pass and the backward products of its 128-wide layers on
+// the tensor cores (mma.sync m16n8k16, bf16 operands, fp32 accumulation), the
+// output layer's backward and Adam in fp32.
 //
 // Network per node: x (128, bf16) -> [W1 x + b1 -> gelu -> bf16] -> [W2 ...]
 // -> [W3 ...] -> W4 h3 + b4 (3 outputs).  The outputs are the deviation of
@@ -325,6 +326,117 @@ __global__ void __launch_bounds__(256) k_wgrad(int n, const float* __restrict__ 
   if (threadIdx.x < DOUT) out[DOUT * D + threadIdx.x] = bacc;
 }
 
+// ---- backward of the 128-wide layers on the tensor cores ----------------------
+// The products take the upstream gradient dZ rounded to bf16 (the weights and
+// activations already are), accumulate in fp32: mma.sync m16n8k16, A row-major
+// 16x16, B col-major 16x8.  Operands are staged transposed in shared memory
+// with padded rows, so every fragment is one 32-bit load without bank conflicts.
+
+// weight gradient partials of a 128x128 layer: part[b][j*128 + k] = sum over the
+// block's rows of dZ[r][j] * Hin[r][k]; part[b][128*128 + j] = sum dZ[r][j] (fp32).
+// 8 warps, warp w owns output rows j = 16w..16w+15, all 128 columns.
+__global__ void __launch_bounds__(256) k_wgrad_tc(int n, const float* __restrict__ dZ, int dz_stride,
+                                                   const __nv_bfloat16* __restrict__ Hin, const int* __restrict__ rows,
+                                                   int rows_per_block, float* __restrict__ part) {
+  constexpr int RP = 40;                   // 32 rows of a chunk + 8 pad (80-byte rows)
+  __shared__ __nv_bfloat16 sdT[D][RP];     // dZ^T of the chunk: [j][r]
+  __shared__ __nv_bfloat16 shT[D][RP];     // Hin^T of the chunk: [k][r]
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, c = lane & 3;
+  float acc[16][4];
+#pragma unroll
+  for (int t = 0; t < 16; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+  float bacc = 0.0f;
+  const int rb = blockIdx.x * rows_per_block, re = min(n, rb + rows_per_block);
+  for (int r0 = rb; r0 < re; r0 += 32) {
+    const int cnt = min(32, re - r0);
+    for (int i = threadIdx.x; i < 32 * D; i += blockDim.x) {
+      const int rr = i / D, j = i % D;
+      float v = 0.0f;
+      __nv_bfloat16 h = __float2bfloat16_rn(0.0f);
+      if (rr < cnt) {
+        v = dZ[(size_t)(r0 + rr) * dz_stride + j];
+        const long long src = rows ? rows[r0 + rr] : (r0 + rr);
+        h = Hin[src * D + j];
+      }
+      sdT[j][rr] = __float2bfloat16_rn(v);
+      shT[j][rr] = h;
+    }
+    if (threadIdx.x < D)
+      for (int rr = 0; rr < cnt; rr++) bacc += dZ[(size_t)(r0 + rr) * dz_stride + threadIdx.x];
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < 2; ks++) {
+      const int kc = 16 * ks + 2 * c;
+      const unsigned a0 = ld_b32(&sdT[16 * w + g][kc]), a1 = ld_b32(&sdT[16 * w + g + 8][kc]);
+      const unsigned a2 = ld_b32(&sdT[16 * w + g][kc + 8]), a3 = ld_b32(&sdT[16 * w + g + 8][kc + 8]);
+#pragma unroll
+      for (int t = 0; t < 16; t++) {
+        const unsigned b0 = ld_b32(&shT[8 * t + g][kc]), b1 = ld_b32(&shT[8 * t + g][kc + 8]);
+        mma_bf16(acc[t], a0, a1, a2, a3, b0, b1);
+      }
+    }
+    __syncthreads();
+  }
+  float* out = part + (size_t)blockIdx.x * (D * D + D);
+#pragma unroll
+  for (int t = 0; t < 16; t++) {
+    const int j0 = 16 * w + g, k0 = 8 * t + 2 * c;
+    out[(size_t)j0 * D + k0] = acc[t][0];
+    out[(size_t)j0 * D + k0 + 1] = acc[t][1];
+    out[(size_t)(j0 + 8) * D + k0] = acc[t][2];
+    out[(size_t)(j0 + 8) * D + k0 + 1] = acc[t][3];
+  }
+  if (threadIdx.x < D) out[D * D + threadIdx.x] = bacc;
+}
+
+// dZprev[r][k] = (sum_j dZ[r][j] W[j][k]) * gelu'(Zprev[r][k]) for a 128x128 layer;
+// W^T staged once per block, 32-row tiles of dZ; warp w: rows 16(w%2).., columns 32(w/2)..
+__global__ void __launch_bounds__(256) k_back_tc(int n, const float* __restrict__ dZ, int dz_stride,
+                                                  const __nv_bfloat16* __restrict__ Wb,
+                                                  const float* __restrict__ Zprev, float* __restrict__ dZprev) {
+  __shared__ __nv_bfloat16 swT[D][KP];     // W^T: [k][j]
+  __shared__ __nv_bfloat16 sa[32][KP];     // dZ rows of the tile: [r][j]
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, c = lane & 3;
+  for (int i = threadIdx.x; i < D * D; i += blockDim.x) swT[i % D][i / D] = Wb[i];
+  const int mt = w & 1, nq = w >> 1;
+  for (int r0 = blockIdx.x * 32; r0 < n; r0 += gridDim.x * 32) {
+    for (int i = threadIdx.x; i < 32 * D; i += blockDim.x) {
+      const int rr = i / D, j = i % D;
+      sa[rr][j] = __float2bfloat16_rn(r0 + rr < n ? dZ[(size_t)(r0 + rr) * dz_stride + j] : 0.0f);
+    }
+    __syncthreads();
+    float acc[4][4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+#pragma unroll
+    for (int ks = 0; ks < D / 16; ks++) {
+      const int kc = 16 * ks + 2 * c;
+      const unsigned a0 = ld_b32(&sa[16 * mt + g][kc]), a1 = ld_b32(&sa[16 * mt + g + 8][kc]);
+      const unsigned a2 = ld_b32(&sa[16 * mt + g][kc + 8]), a3 = ld_b32(&sa[16 * mt + g + 8][kc + 8]);
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int n0 = 32 * nq + 8 * t;
+        const unsigned b0 = ld_b32(&swT[n0 + g][kc]), b1 = ld_b32(&swT[n0 + g][kc + 8]);
+        mma_bf16(acc[t], a0, a1, a2, a3, b0, b1);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const int k = 32 * nq + 8 * t + 2 * c;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int r = r0 + 16 * mt + g + 8 * h;
+        if (r < n) {
+          const size_t o = (size_t)r * D + k;
+          dZprev[o] = acc[t][2 * h] * gelu_grad(Zprev[o]);
+          dZprev[o + 1] = acc[t][2 * h + 1] * gelu_grad(Zprev[o + 1]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // g[w_off + i] = sum_b part[b][i] (i < dout*128), g[b_off + j] = sum_b part[b][doutp*128 + j];
 // a part row holds doutp >= dout output rows (the padded output layer)
 __global__ void k_reduce_parts(int nb, int dout, int doutp, const float* __restrict__ part, float* __restrict__ g,
@@ -484,19 +596,20 @@ rg_status backward(rg_mlp* m, int n, const int* rows, const __nv_bfloat16* X, co
   k_reduce_parts<<<4, 256, 0, m->st>>>(nbw, NOUT, 4, m->spart.p, m->G.p, OFF_W4, OFF_B4);
   const int gbk = grid_of(m, (long long)n, 8);
   k_back<4><<<gbk, 128, 0, m->st>>>(n, m->sdY.p, 4, m->Wb.p + 3 * WB_LAYER, Z + (size_t)2 * n * D, m->sdA.p);
+  const int gbt = std::min((n + 31) / 32, m->num_sms * 4);
   // hidden layers 3, 2: dW_l from h_{l-1}, dZ_{l-1} through W_l
   float* dz = m->sdA.p;
   float* dzn = m->sdB.p;
   for (int l = 3; l >= 2; l--) {
-    k_wgrad<D><<<nbw, 256, 0, m->st>>>(n, dz, D, H + (size_t)(l - 2) * n * D, nullptr, rpb, m->spart.p);
+    k_wgrad_tc<<<nbw, 256, 0, m->st>>>(n, dz, D, H + (size_t)(l - 2) * n * D, nullptr, rpb, m->spart.p);
     const int woff = l == 3 ? OFF_W3 : OFF_W2, boff = l == 3 ? OFF_B3 : OFF_B2;
     k_reduce_parts<<<64, 256, 0, m->st>>>(nbw, D, D, m->spart.p, m->G.p, woff, boff);
-    k_back<D><<<gbk, 128, 0, m->st>>>(n, dz, D, m->Wb.p + (size_t)(l - 1) * WB_LAYER, Z + (size_t)(l - 2) * n * D,
+    k_back_tc<<<gbt, 256, 0, m->st>>>(n, dz, D, m->Wb.p + (size_t)(l - 1) * WB_LAYER, Z + (size_t)(l - 2) * n * D,
                                       dzn);
     std::swap(dz, dzn);
   }
   // first layer: dW1 from the network input
-  k_wgrad<D><<<nbw, 256, 0, m->st>>>(n, dz, D, X, rows, rpb, m->spart.p);
+  k_wgrad_tc<<<nbw, 256, 0, m->st>>>(n, dz, D, X, rows, rpb, m->spart.p);
   k_reduce_parts<<<64, 256, 0, m->st>>>(nbw, D, D, m->spart.p, m->G.p, OFF_W1, OFF_B1);
   MTRY(cudaGetLastError());
   if (loss_sum) {
