@@ -6,8 +6,9 @@ targets and the prediction's extrapolation base; training lowers the loss.
 Tolerances: the GPU sums in fp32 and rounds activations to bf16 exactly like
 the oracle, but a product that lands on a bf16 rounding boundary can round
 the other way, which moves single activations by one bf16 ulp (2^-8
-relative); outputs are compared to 2e-2 of their magnitude, the loss to 1e-2
-relative and each gradient block to 3e-2 in relative 2-norm."""
+relative), and the tensor-core backward rounds the upstream gradient to bf16
+(2^-9 relative per element); outputs are compared to 2e-2 of their magnitude,
+the loss to 1e-2 relative and each gradient block to 3e-2 in relative 2-norm."""
 
 import numpy as np
 import pytest
