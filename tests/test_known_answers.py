@@ -1,0 +1,75 @@
+"""Known-answer checks of the discretisation the path solves, on the oracle's
+restatement of the element assembly (CPU): a lake at rest -- flat water
+surface over a bumpy bed, no flow, no inflow, the outlet level equal to the
+lake level -- is an exact steady solution of the reference's weak form (the
+seven-point rule integrates the hydrostatic terms exactly and the boundary
+lines close the pressure integral), so the assembled residual vanishes to
+rounding while the Jacobian does not."""
+
+import ctypes as C
+
+import numpy as np
+
+import oracle
+from rismo2d_gb300 import deck, meshgen
+from rismo2d_gb300.sim import Params, Simulation, RG_DEVICE_NONE
+
+
+def _system(mesh, params, line_bcs, S, dt=None):
+    sim = Simulation(mesh, params, line_bcs=line_bcs, device=RG_DEVICE_NONE)
+    zero = np.zeros(mesh.np)
+    sim.set_state(zero, zero, S)
+    sim.dry_rewet_pass()
+    s0 = sim.get_state()
+    en = np.ascontiguousarray(mesh.elems, np.int32)
+    mats = {no: n for no, n, _vt in mesh.materials}
+    elem_n = np.ascontiguousarray([mats[int(t)] for t in mesh.elem_type], np.float64)
+    af = np.ones(len(en))
+    cf = np.zeros(mesh.np)
+    nnd = np.full(len(en), 6, np.int32)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)
+    oracle.lib().orc_friction(C.c_int(mesh.np), C.c_int(len(en)), P(en), P(nnd), P(elem_n), P(af), P(s0["U"]),
+                              P(s0["V"]), P(s0["S"]), P(s0["z"]), C.c_double(0.5 * params.dry_limit),
+                              C.c_double(params.g), P(cf))
+    sim.prepare_iteration(0.0, cf)
+    st, num, bnd, mod = sim.get_state(), sim.numbering(), sim.boundary(), sim.model()
+    r = 0.0 if dt is None else 1.0 / dt / params.theta
+    m = oracle.Model(x=mesh.x, y=mesh.y, z=st["z"], U=st["U"], V=st["V"], S=st["S"], dUdt=zero, dVdt=zero,
+                     dSdt=zero, cf=cf, cfw=zero, uu=zero, uv=zero, vv=zero, rot=bnd["rot4"], niox=mod["niox"],
+                     nioy=mod["nioy"], bcU=bnd["bcU"], bcS=bnd["bcS"], evt=mod["elem_vt"], nflag=bnd["nflag"],
+                     bckind=bnd["bckind"], eqno=num["eqno"], enodes=mod["elem_nodes"], ennd=mod["elem_nnd"],
+                     eflag=mod["elem_flag"], g=params.g, hmin=0.5 * params.dry_limit, vk=params.vk,
+                     relaxThdt_UV=r, relaxThdt_H=r)
+    n = num["neq"]
+    ptr = np.zeros(n + 1, np.int64)
+    ptr[1:] = np.cumsum(num["width"])
+    A, B = oracle.assemble(m, ptr, np.ascontiguousarray(num["index"], np.int32), np.float64)
+    sim.close()
+    return A, B
+
+
+def test_lake_at_rest_has_zero_residual():
+    mesh = meshgen.channel(nx=20, ny=4, length=400.0, width=50.0, nbumps=6, seed=5, Q=10.0)
+    S_lake = float(np.max(mesh.z)) + 2.0
+    bcs = [("QINLET", 1, [(0.0, S_lake)]), ("OUTLET", 2, [(S_lake,)])]
+    A, B = _system(mesh, Params(), bcs, np.full(mesh.np, S_lake))
+    H = S_lake - deck.bed_zor(mesh)
+    scale = Params().g * float(np.max(H)) ** 2 * 400.0        # a hydrostatic force times a length
+    assert np.max(np.abs(A)) > 0.0
+    assert np.max(np.abs(B)) <= 1e-12 * scale, np.max(np.abs(B)) / scale
+
+
+def test_lake_at_rest_unsteady_and_with_inflow():
+    """With the time term the lake stays a solution; an inflow breaks the balance
+    only through the inlet rows (specified minus actual discharge)."""
+    mesh = meshgen.channel(nx=20, ny=4, length=400.0, width=50.0, nbumps=6, seed=5, Q=10.0)
+    S_lake = float(np.max(mesh.z)) + 2.0
+    H = S_lake - deck.bed_zor(mesh)
+    scale = Params().g * float(np.max(H)) ** 2 * 400.0
+    _A, B = _system(mesh, Params(), [("QINLET", 1, [(0.0, S_lake)]), ("OUTLET", 2, [(S_lake,)])],
+                    np.full(mesh.np, S_lake), dt=10.0)
+    assert np.max(np.abs(B)) <= 1e-12 * scale
+    _A, B = _system(mesh, Params(), [("QINLET", 1, [(25.0, S_lake)]), ("OUTLET", 2, [(S_lake,)])],
+                    np.full(mesh.np, S_lake))
+    nz = np.flatnonzero(np.abs(B) > 1e-9 * scale)
+    assert 0 < len(nz) <= 2 * (mesh.meta["ny"] * 2 + 1)           # the inlet nodes' rows only
