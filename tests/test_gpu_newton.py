@@ -84,3 +84,25 @@ def test_steady_channel_inexact_newton(name, prec, forcing, reuse):
     stages = sim.stage_ms()
     assert stages["krylov"] > 0.0 and stages["assemble"] > 0.0
     sim.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_lake_at_rest_on_the_gpu(prec):
+    """Known answer: a lake at rest over a bumpy bed (no flow, no inflow, outlet at the lake
+    level) is an exact solution -- the GPU's first Newton residual vanishes to rounding and
+    the step leaves the lake as it was."""
+    from rismo2d_gb300 import deck
+    mesh = meshgen.channel(nx=20, ny=4, length=400.0, width=50.0, nbumps=6, seed=5, Q=10.0)
+    S_lake = float(np.max(mesh.z)) + 2.0
+    bcs = [("QINLET", 1, [(0.0, S_lake)]), ("OUTLET", 2, [(S_lake,)])]
+    sim = Simulation(mesh, Params(max_newton=2), precision=prec, line_bcs=bcs)
+    zero = np.zeros(mesh.np)
+    sim.set_state(zero, zero, np.full(mesh.np, S_lake))
+    rep = sim.step(0.0, 3600.0, steady=True, criterion=RG_CRIT_CORRECTION)
+    H = S_lake - deck.bed_zor(mesh)
+    scale = 9.81 * float(np.max(H)) ** 2 * 400.0
+    assert rep["residual_first"] <= 1e-10 * scale
+    got = sim.get_state()
+    assert np.max(np.abs(got["U"])) <= 1e-9 and np.max(np.abs(got["V"])) <= 1e-9
+    assert np.max(np.abs(got["S"] - S_lake)) <= 1e-9
+    sim.close()
