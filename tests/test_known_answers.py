@@ -1,10 +1,11 @@
 """Known-answer checks of the discretisation the path solves, on the oracle's
 restatement of the element assembly (CPU): a lake at rest -- flat water
 surface over a bumpy bed, no flow, no inflow, the outlet level equal to the
-lake level -- is an exact steady solution of the reference's weak form (the
-seven-point rule integrates the hydrostatic terms exactly and the boundary
-lines close the pressure integral), so the assembled residual vanishes to
-rounding while the Jacobian does not."""
+lake level -- and Manning uniform flow down a plane slope are exact steady
+solutions of the reference's weak form (the seven-point rule integrates the
+hydrostatic terms exactly and the boundary lines close the pressure
+integral), so the assembled residual vanishes to rounding while the Jacobian
+does not."""
 
 import ctypes as C
 
@@ -15,16 +16,31 @@ from rismo2d_gb300 import deck, meshgen
 from rismo2d_gb300.sim import Params, Simulation, RG_DEVICE_NONE
 
 
-def _system(mesh, params, line_bcs, S, dt=None):
+def _area_factors(mesh):
+    """GRID::AreaFactors (ArFact.cpp:41-97): |normal| / n_z of each triangle on the bed zor."""
+    en = np.ascontiguousarray(mesh.elems, np.int32)
+    zor = deck.bed_zor(mesh)
+    cor = en[:, :3]
+    x0, y0, z0 = mesh.x[cor[:, 0]], mesh.y[cor[:, 0]], zor[cor[:, 0]]
+    xx = [mesh.x[cor[:, i]] - x0 for i in (1, 2)]
+    yy = [mesh.y[cor[:, i]] - y0 for i in (1, 2)]
+    zz = [zor[cor[:, i]] - z0 for i in (1, 2)]
+    t1 = yy[0] * zz[1] - yy[1] * zz[0]
+    t2 = zz[0] * xx[1] - zz[1] * xx[0]
+    t3 = xx[0] * yy[1] - xx[1] * yy[0]
+    return np.ascontiguousarray(np.sqrt(t1 * t1 + t2 * t2 + t3 * t3) / t3)
+
+
+def _system(mesh, params, line_bcs, S, dt=None, U=None):
     sim = Simulation(mesh, params, line_bcs=line_bcs, device=RG_DEVICE_NONE)
     zero = np.zeros(mesh.np)
-    sim.set_state(zero, zero, S)
+    sim.set_state(zero if U is None else U, zero, S)
     sim.dry_rewet_pass()
     s0 = sim.get_state()
     en = np.ascontiguousarray(mesh.elems, np.int32)
     mats = {no: n for no, n, _vt in mesh.materials}
     elem_n = np.ascontiguousarray([mats[int(t)] for t in mesh.elem_type], np.float64)
-    af = np.ones(len(en))
+    af = _area_factors(mesh)
     cf = np.zeros(mesh.np)
     nnd = np.full(len(en), 6, np.int32)
     P = lambda a: a.ctypes.data_as(C.c_void_p)
@@ -73,3 +89,22 @@ def test_lake_at_rest_unsteady_and_with_inflow():
                     np.full(mesh.np, S_lake))
     nz = np.flatnonzero(np.abs(B) > 1e-9 * scale)
     assert 0 < len(nz) <= 2 * (mesh.meta["ny"] * 2 + 1)           # the inlet nodes' rows only
+
+
+def test_manning_uniform_flow_has_zero_residual():
+    """Uniform flow down a plane slope: depth H, velocity U with g H S0 = cf U^2, where
+    cf = areaFact g n^2 / H^0.333333 is the reference's nodal Manning coefficient
+    (DoFriction.cpp:87-206) -- U is Manning's H^(2/3) S0^(1/2) / n to 1e-5.  Inlet
+    discharge U H W, outlet level H: the assembled residual vanishes to rounding."""
+    L, W, slope, Hd = 400.0, 50.0, 0.001, 2.0
+    mesh = meshgen.channel(nx=20, ny=4, length=L, width=W, slope=slope, nbumps=0, depth0=Hd)
+    p = Params()
+    n = mesh.materials[0][1]
+    af = float(np.sqrt(1.0 + slope * slope))                 # inclined-element area factor
+    U = float(np.sqrt(p.g * Hd * slope / (af * p.g * n * n / Hd ** 0.333333)))
+    assert abs(U - Hd ** (2.0 / 3.0) * slope ** 0.5 / n) <= 1e-5 * U
+    bcs = [("QINLET", 1, [(U * Hd * W, slope * L + Hd)]), ("OUTLET", 2, [(Hd,)])]
+    A, B = _system(mesh, p, bcs, deck.bed_zor(mesh) + Hd, U=np.full(mesh.np, U))
+    scale = p.g * Hd * slope * (L / 20.0) * (W / 4.0)         # friction / slope force on one quad
+    assert np.max(np.abs(A)) > 0.0
+    assert np.max(np.abs(B)) <= 1e-10 * scale, np.max(np.abs(B)) / scale
