@@ -108,3 +108,69 @@ def test_manning_uniform_flow_has_zero_residual():
     scale = p.g * Hd * slope * (L / 20.0) * (W / 4.0)         # friction / slope force on one quad
     assert np.max(np.abs(A)) > 0.0
     assert np.max(np.abs(B)) <= 1e-10 * scale, np.max(np.abs(B)) / scale
+
+
+def _model(mesh, p, S, U, V, relax):
+    sim = Simulation(mesh, p, device=RG_DEVICE_NONE)
+    sim.set_state(U, V, S)
+    sim.dry_rewet_pass()
+    s0 = sim.get_state()
+    en = np.ascontiguousarray(mesh.elems, np.int32)
+    cf = np.zeros(mesh.np)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)
+    elem_n = np.full(len(en), mesh.materials[0][1])
+    af = _area_factors(mesh)
+    oracle.lib().orc_friction(C.c_int(mesh.np), C.c_int(len(en)), P(en), P(np.full(len(en), 6, np.int32)),
+                              P(elem_n), P(af), P(s0["U"]), P(s0["V"]), P(s0["S"]), P(s0["z"]),
+                              C.c_double(0.5 * p.dry_limit), C.c_double(p.g), P(cf))
+    sim.prepare_iteration(0.0, cf)
+    st, num, bnd, mod = sim.get_state(), sim.numbering(), sim.boundary(), sim.model()
+    Z = lambda: np.zeros(mesh.np)        # separate arrays: the model points into each
+    m = oracle.Model(x=mesh.x, y=mesh.y, z=st["z"], U=st["U"], V=st["V"], S=st["S"], dUdt=Z(), dVdt=Z(),
+                     dSdt=Z(), cf=cf, cfw=Z(), uu=Z(), uv=Z(), vv=Z(), rot=bnd["rot4"], niox=mod["niox"],
+                     nioy=mod["nioy"], bcU=bnd["bcU"], bcS=bnd["bcS"], evt=mod["elem_vt"], nflag=bnd["nflag"],
+                     bckind=bnd["bckind"], eqno=num["eqno"], enodes=mod["elem_nodes"], ennd=mod["elem_nnd"],
+                     eflag=mod["elem_flag"], g=p.g, hmin=0.5 * p.dry_limit, vk=p.vk, relaxThdt_UV=relax,
+                     relaxThdt_H=relax)
+    sim.close()
+    return m, np.asarray(bnd["nflag"]), np.asarray(mod["elem_nodes"]), np.asarray(mod["elem_nnd"])
+
+
+def test_element_jacobian_matches_finite_differences():
+    """EQS_UVS2D::Region's 15x15 Jacobian (CoefsUVS2D.cpp:740-1060) against central
+    differences of its own element residual, on a non-uniform flow over a bumpy bed, for
+    interior triangles, steady and with the time term (the state's time derivative moved
+    with U, V, S at relaxThdt): every block agrees to 1e-8 of the matrix's largest entry
+    when the nodal friction coefficient is held fixed -- the Jacobian is exact apart from
+    the friction coefficient's dependence on the depth, which the reference recomputes
+    every iteration and does not differentiate."""
+    mesh = meshgen.channel(nx=20, ny=4, length=400.0, width=50.0, nbumps=6, seed=5, Q=100.0)
+    p = Params()
+    x, y = mesh.x, mesh.y
+    U = 1.0 + 0.3 * np.sin(x / 50.0) * np.cos(y / 20.0)
+    V = 0.2 * np.sin(x / 30.0)
+    S = deck.bed_zor(mesh) + 2.0 + 0.1 * np.cos(x / 40.0)
+    N_BOUND = 16
+    h = 1e-6
+    for relax in (0.0, 0.1):
+        m, nflag, men, mnnd = _model(mesh, p, S, U, V, relax)
+        interior = [e for e in range(len(mnnd)) if mnnd[e] == 6 and not np.any(nflag[men[e]] & N_BOUND)]
+        assert len(interior) >= 8
+        for e in interior[:8]:
+            _ok, K, _f = oracle.coefs(m, e)
+            nd = men[e]
+            scale = np.max(np.abs(K[:15, :15]))
+            for c in range(15):
+                var, k = c // 6, c % 6
+                if var == 2 and k >= 3:
+                    continue                              # S lives on the corners only
+                arr, drv = ("U", "dUdt") if var == 0 else (("V", "dVdt") if var == 1 else ("S", "dSdt"))
+                fs = []
+                for sgn in (1.0, -1.0):
+                    m.arrays[arr][nd[k]] += sgn * h
+                    m.arrays[drv][nd[k]] += sgn * h * relax
+                    fs.append(oracle.coefs(m, e)[2])
+                    m.arrays[arr][nd[k]] -= sgn * h
+                    m.arrays[drv][nd[k]] -= sgn * h * relax
+                fd = -(fs[0] - fs[1]) / (2.0 * h)
+                assert np.max(np.abs(K[:15, c] - fd[:15])) <= 1e-8 * scale, (relax, e, c)
