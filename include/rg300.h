@@ -101,6 +101,18 @@ rg_status rg_get_state(rg_ctx* ctx, double* U, double* V, double* S, double* z);
  * EqsUVS2D.cpp:105-148). */
 rg_status rg_set_relax(rg_ctx* ctx, double relaxThdt_UV, double relaxThdt_H);
 
+/* Jacobian option, no counterpart in the reference.  friction_depth = 1 adds
+ * to the U-H and V-H blocks the derivative of the bottom friction cf*|U|*U
+ * (cf*|U|*V) with respect to the corner depths through the nodal Manning
+ * coefficient: cf_k = C_k / max(h_k, hmin)^0.333333 (MODEL::DoFriction,
+ * DoFriction.cpp:87-206) gives dcf_k/dh_k = -0.333333 cf_k / h_k above hmin.
+ * The reference's Jacobian (CoefsUVS2D.cpp:749-1059) holds cf fixed, so its
+ * Newton iteration converges only linearly where friction dominates (shallow
+ * water).  The residual is unchanged: the converged solution is the same,
+ * only the Newton path changes.  0 (default) restores the reference's
+ * Jacobian. */
+rg_status rg_set_jacobian(rg_ctx* ctx, int friction_depth);
+
 /* Assemble the Newton system on the GPU (CRSMAT::Init + AssembleEqs_im,
  * CRSMat.cpp:206, Assemble.cpp:195).  Optional outputs (NULL to skip):
  * B (neq doubles) and the matrix values in the reference's packed layout, as
@@ -125,11 +137,11 @@ rg_status rg_ilu0_factor(rg_ctx* ctx, float* LU32_out, double* LU64_out);
 /* PRECO_ILU0::Solve (Preco_ilu0.cpp:497-980) of a host vector. */
 rg_status rg_ilu0_apply(rg_ctx* ctx, const double* B, double* X);
 
-/* PRECO_ILU0::Solve of a DEVICE vector, allocating nothing: x_dev = M^-1 b_dev
- * with the resident factors, for callers that must not allocate during a
- * solve (a caller that pre-plans all device memory, or one whose loop cannot
- * take the implicit synchronisation of cudaMalloc/cudaFree).  No counterpart
- * in the reference.
+/* ILU(0) preconditioner applied to a DEVICE vector without allocating:
+ * x_dev = M^-1 b_dev with the resident factors.  It has no counterpart in the
+ * reference.  It is meant for callers that must not allocate during a solve: a
+ * caller that plans all device memory up front, or one whose loop cannot take
+ * the implicit synchronisation of cudaMalloc/cudaFree.
  *  - The intermediate vector of the two triangular solves is a fixed
  *    file-scope device array of RG_NOALLOC_MAX_EQ doubles (2 MiB); a system
  *    with more equations is rejected with RG_ERR_ARG (use rg_ilu0_apply).
@@ -140,9 +152,10 @@ rg_status rg_ilu0_apply(rg_ctx* ctx, const double* B, double* X);
  *  - All contexts of a process share the one array per device: calls that
  *    overlap in time on the same device (two host threads, or two contexts)
  *    race on it and must be serialised by the caller.
- *  - b_dev and x_dev hold neq doubles each; the call runs on the context's
- *    stream and returns when the result is in x_dev, so b_dev must be
- *    complete when the call is made. */
+ *  - b_dev and x_dev hold neq doubles each and must not overlap (an overlap
+ *    is rejected with RG_ERR_ARG); the call runs on the context's stream and
+ *    returns when the result is in x_dev, so b_dev must be complete when the
+ *    call is made. */
 #define RG_NOALLOC_MAX_EQ (1 << 18)
 rg_status rg_ilu0_apply_dev_noalloc(rg_ctx* ctx, const double* b_dev, double* x_dev);
 
@@ -189,6 +202,16 @@ rg_status rg_newton_update(rg_ctx* ctx, const rg_update_opts* opts, double* stat
  * per-element Manning n and area factor (GRID::AreaFactors ArFact.cpp:41). */
 rg_status rg_set_friction(rg_ctx* ctx, const double* elem_n, const double* elem_areafact);
 rg_status rg_friction(rg_ctx* ctx, double* cf_out);
+
+/* MODEL::Continuity (Contin.cpp:43-170): the discharge through each control
+ * section from the resident state, in FP64 on the device.  seg_nodes holds 3
+ * nodes per line element (corner, corner, mid-side: the control file's
+ * order), seg_section the 1-based section (line) number of each element;
+ * Qx[k], Qy[k] receive the x and y parts of section k+1 (the reference prints
+ * their sum, and each section's share of section 1).  Sums within a section
+ * run in a fixed order. */
+rg_status rg_continuity(rg_ctx* ctx, int nseg, const int* seg_nodes, const int* seg_section, int nsect,
+                        double* Qx, double* Qy);
 
 /* Device-time of the last call's kernels, by stage (ms), for measurement:
  * [0] assembly, [1] scale, [2] factor, [3] BiCGStab total, [4] SpMV (one),

@@ -94,6 +94,11 @@ typedef struct {
    * factors that misses its tolerance (or breaks down) is repeated at once
    * with fresh factors.  No counterpart in the reference. */
   int    ilu_reuse;
+  /* 0: the reference's Jacobian.  1: the Jacobian also carries the depth
+   * derivative of the nodal Manning coefficient (rg_set_jacobian); the
+   * residual, hence the converged solution, is unchanged.  No counterpart in
+   * the reference. */
+  int    friction_jacobian;
 } rg_step_ctl;
 
 typedef struct {
@@ -153,6 +158,11 @@ typedef enum {
   RG_SIM_NSTAGE = 11
 } rg_sim_stage;
 rg_status rg_sim_stage_ms(rg_sim* sim, double* ms, int n, int reset);
+/* MODEL::Continuity (Contin.cpp:43-170) of the simulation's current state on
+ * the GPU in FP64: the discharge through every control line (section k+1 =
+ * line number k+1, nsect = the largest line number).  With nsect_out only
+ * (Qx = Qy = NULL) returns the section count. */
+rg_status rg_sim_continuity(rg_sim* sim, int* nsect_out, double* Qx, double* Qy);
 /* the host part of one Newton iteration's set-up with the given nodal
  * friction (InitBcon at time t_bc, SetLocation, SetNormal, SetRotation,
  * SetEqno when the model changed) -- no GPU work */

@@ -16,6 +16,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
+
+def reference_sources() -> str:
+    """Directory of the reference's C++ sources: $RG_REFERENCE_SOURCES, else the
+    REFSRC default of oracle/Makefile (the recipe that compiles them)."""
+    env = os.environ.get("RG_REFERENCE_SOURCES")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REFSRC"):
+                return line.split("=", 1)[1].strip()
+    return ""
+
 _lib = None
 
 
@@ -155,3 +168,16 @@ def bicgstab(ptr, index, A, ILU, b, maxiter=1000, maxdiff=1e-8, x0=None):
         C.c_int(len(b)), _p(ptr), _p(index), _p(A), _p(ILU), _p(np.ascontiguousarray(b)), _p(x),
         C.c_int(maxiter), C.c_double(maxdiff), C.byref(it), C.byref(acc))
     return ok, x, it.value, acc.value
+
+
+def continuity(seg_nodes, seg_section, nsect, x, y, U, V, S, z):
+    """Discharge through the control sections (MODEL::Continuity, Contin.cpp:43-170)."""
+    L = lib()
+    seg_nodes = np.ascontiguousarray(seg_nodes, np.int32).reshape(-1)
+    seg_section = np.ascontiguousarray(seg_section, np.int32)
+    arrs = [np.ascontiguousarray(a, np.float64) for a in (x, y, U, V, S, z)]
+    qx, qy = np.zeros(nsect), np.zeros(nsect)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)
+    L.orc_continuity(C.c_int(len(seg_section)), P(seg_nodes), P(seg_section), C.c_int(nsect),
+                     *[P(a) for a in arrs], P(qx), P(qy))
+    return qx, qy

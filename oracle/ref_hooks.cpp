@@ -16,6 +16,12 @@
 //
 // Records are written to the file named by $RG_DUMP (nothing is written when it
 // is unset): an 8-byte tag, an int64 payload size, the payload.
+//
+// With $RG_DUMP_LIGHT=1 (large meshes) only small records are written:
+//   SCALE  as above
+//   XL     solver status, BiCGStab count and the wall time of EQS::Solve
+//   ASML   wall time of the assembly
+//   FINALL wall time of the whole time step, then per node U, V, S, z and flag
 
 #define protected public
 #define private public
@@ -77,6 +83,44 @@ struct Rec
 };
 
 static EQS_UVS2D* g_eqs = NULL;    // equation object of the running Newton step
+
+static int light_mode()
+{
+  static int m = -1;
+  if( m < 0 )
+  {
+    const char* p = getenv( "RG_DUMP_LIGHT" );
+    m = ( p && *p == '1' ) ? 1 : 0;
+  }
+  return m;
+}
+
+#include <time.h>
+static double wall_s()
+{
+  struct timespec ts;
+  clock_gettime( CLOCK_MONOTONIC, &ts );
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static void dump_final_light( double seconds, MODEL* model )
+{
+  GRID* rg = model->region;
+  int np = rg->Getnp();
+  Rec r;
+  std::vector<double> U, V, S, z;
+  std::vector<int> flag;
+  for( int n=0; n<np; n++ )
+  {
+    NODE* nd = rg->Getnode(n);
+    U.push_back( nd->v.U );  V.push_back( nd->v.V );  S.push_back( nd->v.S );
+    z.push_back( nd->z );    flag.push_back( nd->flag );
+  }
+  r.put( seconds );
+  r.put( (int32_t)np );
+  r.arr( U ); r.arr( V ); r.arr( S ); r.arr( z ); r.arr( flag );
+  r.write( "FINALL" );
+}
 
 static void dump_state( const char* tag, EQS* eqs, MODEL* model, PROJECT* project )
 {
@@ -217,6 +261,16 @@ void   __real__ZN9EQS_UVS2D7ExecuteEP7PROJECTi( EQS_UVS2D*, PROJECT*, int );
 void __wrap__ZN6CRSMAT14AssembleEqs_imEP3EQSPdP5MODELP7PROJECT( CRSMAT* crs, EQS* eqs, double* vec,
                                                                MODEL* model, PROJECT* project )
 {
+  if( light_mode() )
+  {
+    double t0 = wall_s();
+    __real__ZN6CRSMAT14AssembleEqs_imEP3EQSPdP5MODELP7PROJECT( crs, eqs, vec, model, project );
+    Rec r;
+    r.put( wall_s() - t0 );
+    r.put( (int32_t)crs->m_neq );
+    r.write( "ASML" );
+    return;
+  }
   dump_state( "STATE", eqs, model, project );
 
   __real__ZN6CRSMAT14AssembleEqs_imEP3EQSPdP5MODELP7PROJECT( crs, eqs, vec, model, project );
@@ -252,10 +306,19 @@ int __wrap__ZN3EQS5SolveEP5MODELiPdS2_P7PROJECTP6SOLVERPP6PRECONi( EQS* eqs, MOD
                                                                   double* B, double* X, PROJECT* project,
                                                                   SOLVER* slv, PRECON** pre, int assemble )
 {
+  double t0 = wall_s();
   int err = __real__ZN3EQS5SolveEP5MODELiPdS2_P7PROJECTP6SOLVERPP6PRECONi( eqs, model, neq, B, X, project,
                                                                           slv, pre, assemble );
   SOLVER* s = slv ? slv : project->actualSolver;
   Rec r;
+  if( light_mode() )
+  {
+    r.put( (int32_t)err );
+    r.put( (int32_t)(s ? s->iterCountCG : -1) );
+    r.put( wall_s() - t0 );
+    r.write( "XL" );
+    return err;
+  }
   std::vector<double> x( X, X + neq );
   r.put( (int32_t)err );
   r.put( (int32_t)(s ? s->iterCountCG : -1) );
@@ -267,8 +330,12 @@ int __wrap__ZN3EQS5SolveEP5MODELiPdS2_P7PROJECTP6SOLVERPP6PRECONi( EQS* eqs, MOD
 void __wrap__ZN9EQS_UVS2D7ExecuteEP7PROJECTi( EQS_UVS2D* eqs, PROJECT* project, int steady )
 {
   g_eqs = eqs;
+  double t0 = wall_s();
   __real__ZN9EQS_UVS2D7ExecuteEP7PROJECTi( eqs, project, steady );
-  dump_state( "FINAL", eqs, project->M2D, project );
+  if( light_mode() )
+    dump_final_light( wall_s() - t0, project->M2D );
+  else
+    dump_state( "FINAL", eqs, project->M2D, project );
   g_eqs = NULL;
 }
 

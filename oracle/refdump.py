@@ -98,6 +98,16 @@ def read_dump(path: str) -> list:
             err = c.scalar("<i")
             its = c.scalar("<i")
             rec = {"err": err, "iters": its, "X": c.arr("<f8")}
+        elif tag == "XL":
+            err = c.scalar("<i")
+            its = c.scalar("<i")
+            rec = {"err": err, "iters": its, "seconds": c.scalar("<d")}
+        elif tag == "ASML":
+            rec = {"seconds": c.scalar("<d"), "neq": c.scalar("<i")}
+        elif tag == "FINALL":
+            rec = {"seconds": c.scalar("<d"), "np": c.scalar("<i")}
+            for k, dt in (("U", "<f8"), ("V", "<f8"), ("S", "<f8"), ("z", "<f8"), ("flag", "<i4")):
+                rec[k] = c.arr(dt)
         else:
             raise ValueError(f"unknown record {tag!r}")
         out.append((tag, rec))
@@ -121,3 +131,26 @@ def newton_iterations(records: list) -> list:
         elif tag == "FINAL":
             its.append({"final": rec})
     return its
+
+
+def light_steps(records: list) -> list:
+    """Group the records of a light dump (RG_DUMP_LIGHT=1) into time steps: per step the
+    Newton residual norms, BiCGStab counts, solve and assembly seconds, equation counts,
+    the step's wall time and its end state."""
+    steps, cur = [], None
+    for tag, rec in records:
+        if cur is None:
+            cur = {"scales": [], "iters": [], "solve_s": [], "assemble_s": [], "neq": []}
+        if tag == "SCALE":
+            cur["scales"].append(rec["scale"])
+        elif tag == "XL":
+            cur["iters"].append(rec["iters"])
+            cur["solve_s"].append(rec["seconds"])
+        elif tag == "ASML":
+            cur["assemble_s"].append(rec["seconds"])
+            cur["neq"].append(rec["neq"])
+        elif tag == "FINALL":
+            cur.update(rec)
+            steps.append(cur)
+            cur = None
+    return steps

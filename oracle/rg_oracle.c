@@ -653,3 +653,39 @@ void orc_friction(int np, int ne_region, const int* region_nodes, const int* reg
   for( int i=0; i<np; i++ ) if( counter[i] ) cf[i] /= counter[i];
   free( counter );
 }
+
+
+/* MODEL::Continuity (Contin.cpp:83-170): for every control element in order and
+ * every Gauss point of the quadratic line (GPdeg 5: 3 points, Shape.cpp:176-177,
+ * 220-242; SHAPE::shapeOfLine, Line.cpp:43-160): the unnormalised normal
+ * (dN.y, -dN.x), H = M.(S - z) clipped at 0, U and V with the quadratic shape,
+ * Qx += w H U nx, Qy += w H V ny (no MPI interfaces here). */
+void orc_continuity(int nseg, const int* seg_nodes, const int* seg_section, int nsect, const double* x,
+                    const double* y, const double* U, const double* V, const double* S, const double* z,
+                    double* Qx, double* Qy)
+{
+  const double loc[3] = { -sqrt(0.6), 0.0, sqrt(0.6) };
+  const double wgt[3] = { 5.0/9.0, 8.0/9.0, 5.0/9.0 };
+  for( int i=0; i<nsect; i++ ) Qx[i] = Qy[i] = 0.0;
+  for( int e=0; e<nseg; e++ )
+  {
+    int n = seg_section[e];
+    const int* nd = seg_nodes + 3*e;
+    for( int g=0; g<3; g++ )
+    {
+      double xg = loc[g];
+      double M[2]  = { (1.0 - xg) / 2.0, (1.0 + xg) / 2.0 };
+      double N[3]  = { xg * (xg - 1.0) / 2.0, xg * (xg + 1.0) / 2.0, 1.0 - xg * xg };
+      double dN[3] = { xg - 0.5, xg + 0.5, -2.0 * xg };
+      double nx =  dN[0]*y[nd[0]] + dN[1]*y[nd[1]] + dN[2]*y[nd[2]];
+      double ny = -dN[0]*x[nd[0]] - dN[1]*x[nd[1]] - dN[2]*x[nd[2]];
+      double H = M[0] * (S[nd[0]] - z[nd[0]]) + M[1] * (S[nd[1]] - z[nd[1]]);
+      if( H <= 0.0 ) H = 0.0;
+      double u = N[0]*U[nd[0]] + N[1]*U[nd[1]] + N[2]*U[nd[2]];
+      double v = N[0]*V[nd[0]] + N[1]*V[nd[1]] + N[2]*V[nd[2]];
+      double w = wgt[g];
+      Qx[n-1] += w * H * u * nx;
+      Qy[n-1] += w * H * v * ny;
+    }
+  }
+}

@@ -103,6 +103,13 @@ void orc_friction(int np, int ne_region, const int* region_nodes, const int* reg
                   const double* V, const double* S, const double* z, double hmin, double g,
                   double* cf);
 
+/* discharge through the control sections (MODEL::Continuity, Contin.cpp:43-170):
+ * control line elements in file order, 3 Gauss points each; section of element t
+ * is seg_section[t] (1-based); Qx, Qy: nsect sums */
+void orc_continuity(int nseg, const int* seg_nodes, const int* seg_section, int nsect, const double* x,
+                    const double* y, const double* U, const double* V, const double* S, const double* z,
+                    double* Qx, double* Qy);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,9 +28,9 @@ PREC_MIXED = 2
 
 # every symbol the public header declares (checked by the CPU test suite)
 EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pattern", "rg_set_boundary",
-           "rg_set_state", "rg_get_state", "rg_set_relax", "rg_assemble", "rg_load_system", "rg_scale",
+           "rg_set_state", "rg_get_state", "rg_set_relax", "rg_set_jacobian", "rg_assemble", "rg_load_system", "rg_scale",
            "rg_ilu0_factor", "rg_ilu0_apply", "rg_spmv", "rg_bicgstab", "rg_solve", "rg_set_update_lists",
-           "rg_newton_update", "rg_set_friction", "rg_friction", "rg_get_timings",
+           "rg_newton_update", "rg_set_friction", "rg_friction", "rg_continuity", "rg_get_timings",
            "rg_sim_create", "rg_sim_destroy", "rg_sim_last_error", "rg_sim_set_state", "rg_sim_get_state",
            "rg_sim_step", "rg_sim_prepare_iteration", "rg_sim_get_numbering", "rg_sim_get_pattern",
            "rg_sim_get_boundary", "rg_set_elements", "rg_set_old", "rg_get_dt", "rg_timegrad",
@@ -40,7 +40,7 @@ EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pat
            "rg_mlp_create", "rg_mlp_destroy", "rg_mlp_last_error", "rg_mlp_set_mesh", "rg_mlp_set_scales",
            "rg_mlp_get_params", "rg_mlp_set_params", "rg_mlp_features", "rg_mlp_add_samples",
            "rg_mlp_clear_samples", "rg_mlp_train", "rg_mlp_loss_grad", "rg_mlp_predict",
-           "rg_sim_set_warm_start", "rg_sim_stage_ms"]
+           "rg_sim_set_warm_start", "rg_sim_stage_ms", "rg_sim_continuity"]
 
 
 class RgMesh(C.Structure):

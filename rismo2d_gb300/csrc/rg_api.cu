@@ -96,7 +96,7 @@ cudaError_t prof_end(rg_ctx* c) {
   return e;
 }
 
-static rg_status check_device_error(rg_ctx* c) {
+rg_status check_device_error(rg_ctx* c) {
   TRY(d2h(c, c->err_host, c->dev_err.p, 4 * sizeof(int)));
   TRY(cudaStreamSynchronize(c->st));
   int e = c->err_host[0];
@@ -740,6 +740,13 @@ rg_status rg_set_relax(rg_ctx* c, double relaxThdt_UV, double relaxThdt_H) {
   return RG_OK;
 }
 
+rg_status rg_set_jacobian(rg_ctx* c, int friction_depth) {
+  if (!c) return RG_ERR_ARG;
+  if (friction_depth != 0 && friction_depth != 1) return rg_fail(c, RG_ERR_ARG, "rg_set_jacobian: option is 0 or 1");
+  c->jac_friction = friction_depth;
+  return RG_OK;
+}
+
 static rg_status copy_out_system(rg_ctx* c, double* B_out, float* A32_out, double* A64_out, bool lu) {
   if (B_out) TRY(rg_copy(c, B_out, c->B.p, c->neq * sizeof(double), cudaMemcpyDeviceToHost));
   if (c->prec == RG_PREC_FP64) {
@@ -996,6 +1003,97 @@ rg_status rg_friction(rg_ctx* c, double* cf_out) {
   float ms = 0;
   TRY(cudaEventElapsedTime(&ms, c->ev[14], c->ev[15]));
   c->t_ms[7] = ms;
+  return RG_OK;
+}
+
+// ---- MODEL::Continuity (Contin.cpp:43-170): discharge through control sections
+namespace {
+// one block per section; thread t integrates a contiguous run of the section's
+// line elements in order, then the block sums the runs in a fixed tree order, so
+// the result does not depend on timing.  Three Gauss points (GPdeg 5), quadratic
+// U, V and linear depth (clipped at 0) along the line, the unnormalised normal
+// (dN.y, -dN.x) (SHAPE::shapeOfLine, Line.cpp:43-160).
+__global__ void k_continuity(int nsect, const int* __restrict__ sec_ptr, const int* __restrict__ seg,
+                             const double* __restrict__ x, const double* __restrict__ y,
+                             const double* __restrict__ U, const double* __restrict__ V,
+                             const double* __restrict__ S, const double* __restrict__ z, double* __restrict__ q) {
+  __shared__ double sx[256], sy[256];
+  const int k = blockIdx.x;
+  if (k >= nsect) return;
+  const int b = sec_ptr[k], e = sec_ptr[k + 1], cnt = e - b;
+  const int per = (cnt + blockDim.x - 1) / blockDim.x;
+  const int lo = b + threadIdx.x * per, hi = min(e, lo + per);
+  const double gx = sqrt(0.6);
+  const double gp[3] = {-gx, 0.0, gx}, gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+  double qx = 0.0, qy = 0.0;
+  for (int t = lo; t < hi; t++) {
+    const int n0 = seg[3 * t], n1 = seg[3 * t + 1], n2 = seg[3 * t + 2];
+    for (int g = 0; g < 3; g++) {
+      const double xg = gp[g];
+      const double M0 = (1.0 - xg) / 2.0, M1 = (1.0 + xg) / 2.0;
+      const double N0 = xg * (xg - 1.0) / 2.0, N1 = xg * (xg + 1.0) / 2.0, N2 = 1.0 - xg * xg;
+      const double d0 = xg - 0.5, d1 = xg + 0.5, d2 = -2.0 * xg;
+      const double nx = d0 * y[n0] + d1 * y[n1] + d2 * y[n2];
+      const double ny = -d0 * x[n0] - d1 * x[n1] - d2 * x[n2];
+      double H = M0 * (S[n0] - z[n0]) + M1 * (S[n1] - z[n1]);
+      if (H <= 0.0) H = 0.0;
+      const double u = N0 * U[n0] + N1 * U[n1] + N2 * U[n2];
+      const double v = N0 * V[n0] + N1 * V[n1] + N2 * V[n2];
+      qx += gw[g] * H * u * nx;
+      qy += gw[g] * H * v * ny;
+    }
+  }
+  sx[threadIdx.x] = qx;
+  sy[threadIdx.x] = qy;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      sx[threadIdx.x] += sx[threadIdx.x + o];
+      sy[threadIdx.x] += sy[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    q[2 * k] = sx[0];
+    q[2 * k + 1] = sy[0];
+  }
+}
+}  // namespace
+
+rg_status rg_continuity(rg_ctx* c, int nseg, const int* seg_nodes, const int* seg_section, int nsect, double* Qx,
+                        double* Qy) {
+  if (!c || nseg < 0 || nsect <= 0 || (nseg > 0 && (!seg_nodes || !seg_section)) || !Qx || !Qy)
+    return rg_fail(c, RG_ERR_ARG, "rg_continuity: bad arguments");
+  TRY(cudaSetDevice(c->device));
+  // sort the line elements by section (stable: each section keeps the control file's order)
+  std::vector<int> ptr(nsect + 1, 0), nodes(3 * (size_t)nseg);
+  for (int t = 0; t < nseg; t++) {
+    const int k = seg_section[t] - 1;
+    if (k < 0 || k >= nsect) return rg_fail(c, RG_ERR_ARG, "rg_continuity: section number out of range");
+    for (int i = 0; i < 3; i++)
+      if (seg_nodes[3 * t + i] < 0 || seg_nodes[3 * t + i] >= c->np)
+        return rg_fail(c, RG_ERR_ARG, "rg_continuity: node out of range");
+    ptr[k + 1]++;
+  }
+  for (int k = 0; k < nsect; k++) ptr[k + 1] += ptr[k];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int t = 0; t < nseg; t++) {
+    const int d = fill[seg_section[t] - 1]++;
+    for (int i = 0; i < 3; i++) nodes[3 * (size_t)d + i] = seg_nodes[3 * t + i];
+  }
+  TRY(upload(c, c->sec_ptr, ptr.data(), ptr.size()));
+  TRY(upload(c, c->sec_nodes, nodes.data(), nodes.size()));
+  TRY(c->sec_q.alloc(2 * (size_t)nsect));
+  k_continuity<<<nsect, 256, 0, rg_counted(c)>>>(nsect, c->sec_ptr.p, c->sec_nodes.p, c->x.p, c->y.p, c->U.p, c->V.p,
+                                                  c->S.p, c->z.p, c->sec_q.p);
+  TRY(cudaGetLastError());
+  std::vector<double> q(2 * (size_t)nsect);
+  TRY(d2h(c, q.data(), c->sec_q.p, q.size() * sizeof(double)));
+  TRY(cudaStreamSynchronize(c->st));
+  for (int k = 0; k < nsect; k++) {
+    Qx[k] = q[2 * k];
+    Qy[k] = q[2 * k + 1];
+  }
   return RG_OK;
 }
 

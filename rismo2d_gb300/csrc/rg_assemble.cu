@@ -104,6 +104,7 @@ struct AsmArgs {
   int bcount;
   double g, hmin, vk, rUV, rH;
   const double* geo;   // k_geometry output, per element of the list
+  int jac_friction;    // add the depth derivative of the friction coefficient to the U-H / V-H blocks
 };
 
 // block-coefficient slots per Gauss point
@@ -118,6 +119,7 @@ enum {
   C_SU0, C_SUX,                          // U-derivative of continuity
   C_SV0, C_SVY,                          // V-derivative of continuity
   C_SH0, C_SHX, C_SHY,                   // H-derivative of continuity
+  C_UF, C_VF,                            // friction force per unit cf (w |U| U, w |U| V)
   C_N
 };
 
@@ -214,11 +216,14 @@ __device__ __forceinline__ void block_coefs(KT* c, R w, R H, R U, R V, R dUdx, R
   c[C_SH0] = (KT)(w * rH + w * (dUdx + dVdy));
   c[C_SHX] = (KT)(w * U);
   c[C_SHY] = (KT)(w * V);
+  c[C_UF] = (KT)(w * Ures * U);
+  c[C_VF] = (KT)(w * Ures * V);
 }
 
 template <class KT>
 struct GpData {              // node data and Gauss-point results of one element
   double nd[10][6];          // per node: U V dUdt dVdt S z dSdt cf x y
+  KT dcf[3];                 // corner depth derivatives of cf (0 unless jac_friction)
   double dndx[7][6], dndy[7][6], dmdx[7][3], dmdy[7][3];
   double res[7][7];          // per GP: ffU fxU fyU ffV fxV fyV fC (already times weight)
   KT coef[7][C_N];
@@ -389,6 +394,11 @@ __global__ void __launch_bounds__(WARPS * 32, 6) k_element(AsmArgs a, KT* __rest
       d.nd[7][i] = a.cf[k];
       d.nd[8][i] = a.x[k];
       d.nd[9][i] = a.y[k];
+      if (i < 3) {
+        // d cf_k / d h_k of cf_k = C_k / max(h_k, hmin)^0.333333 (k_friction)
+        const double h = d.nd[4][i] - d.nd[5][i];
+        d.dcf[i] = (a.jac_friction && h > a.hmin) ? (KT)(-0.333333 * d.nd[7][i] / h) : (KT)0;
+      }
     }
     __syncwarp();
 
@@ -510,7 +520,7 @@ __global__ void __launch_bounds__(WARPS * 32, 6) k_element(AsmArgs a, KT* __rest
           case 2:  // U row, H col (corners)
             if (k < 3) {
               KT mk = shape_m<KT>(g, k);
-              t = c[C_UH0] * mk;
+              t = (c[C_UH0] + c[C_UF] * d.dcf[k]) * mk;
               tx = c[C_UHX] * mk;
               ty = c[C_UHY] * mk;
             }
@@ -527,7 +537,7 @@ __global__ void __launch_bounds__(WARPS * 32, 6) k_element(AsmArgs a, KT* __rest
           case 5:  // V row, H col
             if (k < 3) {
               KT mk = shape_m<KT>(g, k);
-              t = c[C_VH0] * mk;
+              t = (c[C_VH0] + c[C_VF] * d.dcf[k]) * mk;
               tx = c[C_VHX] * mk;
               ty = c[C_VHY] * mk;
             }
@@ -751,6 +761,7 @@ cudaError_t launch_assemble(rg_ctx* c) {
   a.nflag = c->nflag.p; a.bckind = c->bckind.p; a.rot = c->rot.p; a.niox = c->niox.p; a.nioy = c->nioy.p;
   a.bcU = c->bcU.p; a.bcS = c->bcS.p; a.enodes = c->enodes.p; a.eflag = c->eflag.p;
   a.evt = c->evt.p; a.g = c->g; a.hmin = c->hmin; a.vk = c->vk; a.rUV = c->rUV; a.rH = c->rH;
+  a.jac_friction = c->jac_friction;
   a.elems = c->color_elem.p;
   a.reg = c->asm_reg.p;
   a.count = c->n_asm_reg;

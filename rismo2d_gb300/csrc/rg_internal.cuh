@@ -132,6 +132,7 @@ struct rg_ctx {
   // mesh and constants
   int np = 0, ne = 0;
   double g = 9.81, hmin = 0.0, vk = 0.0, rUV = 0.0, rH = 0.0;
+  int jac_friction = 0;       // rg_set_jacobian: depth derivative of the friction coefficient
   DBuf<double> x, y, evt;
   DBuf<int> enodes, ennd, eflag;
   std::vector<int> h_enodes, h_ennd, h_eflag, h_region_nodes;
@@ -199,6 +200,11 @@ struct rg_ctx {
   DBuf<double> fr_phmin;         // hmin^0.333333 as the friction kernel's pow gives it
   double fr_phmin_h = -1.0;      // the hmin it was computed for
 
+  // continuity sections (rg_continuity): line elements sorted by section
+  DBuf<int> sec_nodes, sec_ptr;
+  DBuf<double> sec_q;
+  int n_sec = 0;
+
   // timings
   cudaEvent_t ev[16];
   double t_ms[10] = {0};   // device ms by stage; [8] / [9] host ms of the last / all rg_set_pattern calls
@@ -250,6 +256,13 @@ cudaError_t prof_flush(rg_ctx* c);
 // ---- launchers implemented in the .cu files -------------------------------
 rg_status rg_fail(rg_ctx* c, rg_status s, const char* msg);
 rg_status rg_cuda(rg_ctx* c, cudaError_t e, const char* where);
+// read and clear the device error word; maps its bits to a status (rg_api.cu)
+rg_status check_device_error(rg_ctx* c);
+
+// Launch attributes and occupancy figures are properties of a device: a
+// process may drive contexts on several GPUs, so they are cached per device.
+constexpr int kMaxDevices = 64;
+inline bool device_slot_ok(const rg_ctx* c) { return c->device >= 0 && c->device < kMaxDevices; }
 
 // assembly (rg_assemble.cu)
 cudaError_t launch_assemble(rg_ctx* c);

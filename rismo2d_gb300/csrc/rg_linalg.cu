@@ -822,7 +822,9 @@ static cudaError_t launch_factor_t(rg_ctx* c, const MT* A, MT* LU) {
 
 template <class MT, int WARPS>
 static cudaError_t launch_factor_level_t(rg_ctx* c, const MT* A, MT* LU) {
-  static int per_sm = 0;
+  static int per_sm_dev[kMaxDevices] = {0};
+  if (!device_slot_ok(c)) return cudaErrorInvalidDevice;
+  int& per_sm = per_sm_dev[c->device];
   cudaError_t e;
   if (per_sm == 0) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_level<MT, WARPS>, WARPS * 32, 0);
@@ -850,7 +852,9 @@ cudaError_t launch_factor(rg_ctx* c) {
 
 template <class MT, int WARPS, int STAGE>
 static cudaError_t launch_factor_level2_t(rg_ctx* c, const MT* A, MT* LU) {
-  static int per_sm = 0;
+  static int per_sm_dev[kMaxDevices] = {0};
+  if (!device_slot_ok(c)) return cudaErrorInvalidDevice;
+  int& per_sm = per_sm_dev[c->device];
   cudaError_t e;
   if (per_sm == 0) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_level2<MT, WARPS, STAGE>, WARPS * 32, 0);
@@ -910,8 +914,9 @@ template <class VT, class MT, bool LOWER>
 static cudaError_t launch_trsv_t(rg_ctx* c, const MT* val, const MT* diag, const VT* b, VT* x,
                                  const KrylovScalars* ks) {
   constexpr int W = 8;
-  static int per_sm_cache[2][2][2] = {{{0}}};
-  int& per_sm = per_sm_cache[sizeof(VT) == 8][sizeof(MT) == 8][LOWER];
+  static int per_sm_dev[kMaxDevices] = {0};
+  if (!device_slot_ok(c)) return cudaErrorInvalidDevice;
+  int& per_sm = per_sm_dev[c->device];   // one cache per template instantiation and device
   cudaError_t e;
   if (per_sm == 0) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv<VT, MT, LOWER, W>, W * 32, 0);

@@ -559,13 +559,15 @@ cudaError_t refresh_bf16(rg_mlp* m) {
 }
 
 cudaError_t forward(rg_mlp* m, int n, const int* rows, const __nv_bfloat16* X, float* Y, bool store) {
-  static bool attr = false;
-  if (!attr) {
+  // the shared-memory attribute is a property of the device: set it once per device
+  static bool attr[kMaxDevices] = {false};
+  if (m->device < 0 || m->device >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (!attr[m->device]) {
     cudaError_t e = cudaFuncSetAttribute(k_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FWD_SMEM);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr[m->device] = true;
   }
   const int ntiles = (n + TILE - 1) / TILE;
   const int grid = std::max(1, std::min(ntiles, m->num_sms));

@@ -1196,6 +1196,16 @@ rg_status rg_sim_stage_ms(rg_sim* s, double* ms, int n, int reset) {
   return RG_OK;
 }
 
+rg_status rg_sim_continuity(rg_sim* s, int* nsect_out, double* Qx, double* Qy) {
+  if (!s || !s->ctx) return RG_ERR_ARG;
+  int nsect = 0;
+  for (int l : s->seg_line) nsect = std::max(nsect, l);
+  if (nsect_out) *nsect_out = nsect;
+  if (!Qx && !Qy) return RG_OK;
+  if (!Qx || !Qy || nsect == 0) return sfail(s, RG_ERR_ARG, "rg_sim_continuity: no control lines or no output");
+  return rg_continuity(s->ctx, (int)s->seg_line.size(), s->seg_nodes.data(), s->seg_line.data(), nsect, Qx, Qy);
+}
+
 rg_status rg_sim_set_warm_start(rg_sim* s, const double* U, const double* V, const double* S) {
   if (!s || !s->have_state) return RG_ERR_ARG;
   if (!U || !V || !S) {
@@ -1223,6 +1233,8 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
     rUV = rH = 1.0 / dt / th;
   }
   rg_status st = rg_set_relax(s->ctx, rUV, rH);
+  if (st != RG_OK) return st;
+  st = rg_set_jacobian(s->ctx, ctl->friction_jacobian ? 1 : 0);
   if (st != RG_OK) return st;
   // Predict (EqsUVS2D.cpp:1101-1178)
   for (int n = 0; n < s->np; n++) s->dUdt[n] = s->dVdt[n] = s->dSdt[n] = 0.0;

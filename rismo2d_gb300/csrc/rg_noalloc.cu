@@ -15,7 +15,6 @@ namespace {
 static __device__ __align__(256) double g_noalloc_scratch[RG_NOALLOC_MAX_EQ];
 
 // address of the scratch array, looked up once per device
-constexpr int kMaxDevices = 64;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 }  // namespace
@@ -31,7 +30,16 @@ extern "C" rg_status rg_ilu0_apply_dev_noalloc(rg_ctx* c, const double* b_dev, d
   }
   if (!c->have_factor || !b_dev || !x_dev)
     return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply_dev_noalloc: no factors or a NULL vector");
-  if (c->device < 0 || c->device >= kMaxDevices) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply_dev_noalloc: device");
+  {
+    // the dependency-driven solves overwrite x with sentinels before reading b: the
+    // two vectors must not overlap
+    const char* b0 = reinterpret_cast<const char*>(b_dev);
+    const char* x0 = reinterpret_cast<const char*>(x_dev);
+    const size_t bytes = (size_t)c->neq * sizeof(double);
+    if (b0 < x0 + bytes && x0 < b0 + bytes)
+      return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply_dev_noalloc: b_dev and x_dev overlap");
+  }
+  if (!device_slot_ok(c)) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply_dev_noalloc: device");
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return rg_cuda(c, e, "cudaSetDevice");
   if (!g_scratch_ptr[c->device]) {
@@ -42,17 +50,7 @@ extern "C" rg_status rg_ilu0_apply_dev_noalloc(rg_ctx* c, const double* b_dev, d
   }
   e = launch_ilu_apply_w(c, b_dev, g_scratch_ptr[c->device], x_dev);
   if (e != cudaSuccess) return rg_cuda(c, e, "rg_ilu0_apply_dev_noalloc launch");
-  // the context's pinned error word (allocated with the context) reports waits that ran out
-  e = cudaMemcpyAsync(c->err_host, c->dev_err.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-  if (e != cudaSuccess) return rg_cuda(c, e, "rg_ilu0_apply_dev_noalloc sync");
-  if (c->err_host[0] != 0) {
-    char msg[160];
-    snprintf(msg, sizeof msg, "rg_ilu0_apply_dev_noalloc: device wait gave up (kernel %d: row %d waited for %d)",
-             c->err_host[1], c->err_host[2], c->err_host[3]);
-    cudaMemsetAsync(c->dev_err.p, 0, 4 * sizeof(int), c->st);
-    cudaStreamSynchronize(c->st);
-    return rg_fail(c, RG_ERR_DEVICE_WAIT, msg);
-  }
-  return RG_OK;
+  // the context's pinned error word (allocated with the context) reports waits that ran
+  // out, zero pivots and rows that are too wide; it is read and cleared here
+  return check_device_error(c);
 }

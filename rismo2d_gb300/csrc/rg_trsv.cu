@@ -283,12 +283,13 @@ __global__ void k_pack_wave(int nent, const long long* __restrict__ ent_dst, con
 
 template <class VT, bool LOWER, int G, bool FAR>
 static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScalars* ks, size_t smem) {
-  static int attr_done = 0;
-  if (attr_done < (int)smem) {
+  static int attr_done[kMaxDevices] = {0};   // per device: the attribute is a device property
+  if (!device_slot_ok(c)) return cudaErrorInvalidDevice;
+  if (attr_done[c->device] < (int)smem) {
     cudaError_t e = cudaFuncSetAttribute(k_trsv_wave<VT, LOWER, G, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    attr_done = (int)smem;
+    attr_done[c->device] = (int)smem;
   }
   k_trsv_wave<VT, LOWER, G, FAR><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, x,
                                                                       wd.stage_bytes, c->dev_err.p, ks);

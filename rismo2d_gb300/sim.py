@@ -44,7 +44,7 @@ class Deck(C.Structure):
 class StepCtl(C.Structure):
     _fields_ = [("steady", C.c_int), ("first_step", C.c_int), ("criterion", C.c_int),
                 ("residual_tol", C.c_double), ("max_newton", C.c_int), ("linear_forcing", C.c_double),
-                ("ilu_reuse", C.c_int)]
+                ("ilu_reuse", C.c_int), ("friction_jacobian", C.c_int)]
 
 
 class StepReport(C.Structure):
@@ -201,9 +201,9 @@ class Simulation:
 
     def step(self, t: float, dt: float, steady: bool = False, criterion: int = RG_CRIT_RESIDUAL,
              residual_tol: float = 1e-8, max_newton: int = 0, linear_forcing: float = 0.0,
-             ilu_reuse: int = 0) -> dict:
+             ilu_reuse: int = 0, friction_jacobian: bool = False) -> dict:
         ctl = StepCtl(1 if steady else 0, 1 if self.step_no == 0 else 0, criterion, residual_tol, max_newton,
-                      linear_forcing, ilu_reuse)
+                      linear_forcing, ilu_reuse, 1 if friction_jacobian else 0)
         rep = StepReport()
         st = self.lib.rg_sim_step(self.ptr, C.c_double(t), C.c_double(dt), C.byref(ctl), C.byref(rep))
         if st not in (_lib.RG_OK, _lib.RG_NOT_CONVERGED):
@@ -221,6 +221,19 @@ class Simulation:
         if st != _lib.RG_OK:
             raise _lib.RgError(st, "rg_sim_stage_ms")
         return dict(zip(self.STAGES, ms.tolist()))
+
+    def continuity(self) -> dict:
+        """MODEL::Continuity (Contin.cpp:43-170) of the current state, FP64 on the GPU:
+        per control line k+1 the discharge Q = Qx + Qy and its parts."""
+        ns = C.c_int()
+        st = self.lib.rg_sim_continuity(self.ptr, C.byref(ns), None, None)
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_continuity: " + self._err())
+        qx, qy = np.zeros(ns.value), np.zeros(ns.value)
+        st = self.lib.rg_sim_continuity(self.ptr, None, p(qx), p(qy))
+        if st != _lib.RG_OK:
+            raise _lib.RgError(st, "rg_sim_continuity: " + self._err())
+        return {"Q": qx + qy, "Qx": qx, "Qy": qy}
 
     # -- inspection of the host model (numbering, pattern, boundary data) ----
     def prepare_iteration(self, t_bc: float, cf=None):

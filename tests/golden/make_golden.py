@@ -8,7 +8,8 @@ and the correction X -- plus the converged state.
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden.py [--reference /root/reference/sources]
+    python tests/golden/make_golden.py [--reference DIR]   (default: $RG_REFERENCE_SOURCES,
+                                                           else oracle/Makefile's REFSRC)
 
 The fixtures are the reference's own outputs; the oracle (oracle/rg_oracle.c)
 and the CUDA path are checked against them.
@@ -29,6 +30,7 @@ REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
 sys.path.insert(0, REPO)
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
+import oracle  # noqa: E402
 import refdump  # noqa: E402
 from rismo2d_gb300 import deck, meshgen  # noqa: E402
 
@@ -111,7 +113,7 @@ def pack(its: list, keep: list) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference/sources")
+    ap.add_argument("--reference", default=oracle.reference_sources())
     args = ap.parse_args()
     with tempfile.TemporaryDirectory() as tmp:
         # small steady channel: every Newton iteration kept

@@ -6,13 +6,14 @@ reference sources, so it is skipped where they are absent."""
 import os
 import subprocess
 
+import oracle
 import pytest
 
 REPO = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
-REFSRC = "/root/reference/sources"
+REFSRC = oracle.reference_sources()
 
 
-@pytest.mark.skipif(not os.path.isdir(REFSRC), reason="reference sources not present")
+@pytest.mark.skipif(not REFSRC or not os.path.isdir(REFSRC), reason="reference sources not present")
 def test_shim_links_into_reference():
     lib = os.path.join(REPO, "rismo2d_gb300", "librg300.so")
     if not os.path.exists(lib):
