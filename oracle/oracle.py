@@ -181,3 +181,17 @@ def continuity(seg_nodes, seg_section, nsect, x, y, U, V, S, z):
     L.orc_continuity(C.c_int(len(seg_section)), P(seg_nodes), P(seg_section), C.c_int(nsect),
                      *[P(a) for a in arrs], P(qx), P(qy))
     return qx, qy
+
+
+def pattern(np_, enodes, eqno, neq):
+    """CRS pattern in the layout of EQS::SetIndexMat (IndexMat.cpp:91-342) for six-node
+    elements `enodes` (ne, 6) and equation numbers `eqno` (np, 3; -1 none)."""
+    L = lib()
+    L.orc_pattern.restype = C.c_int64
+    en = np.ascontiguousarray(enodes, np.int32).reshape(-1)
+    eq = np.ascontiguousarray(eqno, np.int32).reshape(-1)
+    ptr = np.zeros(neq + 1, np.int64)
+    nnz = L.orc_pattern(C.c_int(np_), C.c_int(len(en) // 6), _p(en), _p(eq), C.c_int(neq), _p(ptr), None)
+    idx = np.zeros(nnz, np.int32)
+    L.orc_pattern(C.c_int(np_), C.c_int(len(en) // 6), _p(en), _p(eq), C.c_int(neq), _p(ptr), _p(idx))
+    return ptr, idx

@@ -689,3 +689,74 @@ void orc_continuity(int nseg, const int* seg_nodes, const int* seg_section, int 
     }
   }
 }
+
+
+int64_t orc_pattern(int np, int ne, const int* enodes, const int* eqno, int neq, int64_t* ptr, int* idx)
+{
+  /* node -> elements holding it, in element order */
+  int64_t* nptr = (int64_t*)calloc( (size_t)np + 1, sizeof(int64_t) );
+  for( int e=0; e<ne; e++ )
+    for( int i=0; i<6; i++ ) nptr[enodes[6*e+i] + 1]++;
+  for( int n=0; n<np; n++ ) nptr[n+1] += nptr[n];
+  int* nel = (int*)malloc( (size_t)nptr[np] * sizeof(int) );
+  int64_t* fill = (int64_t*)malloc( (size_t)np * sizeof(int64_t) );
+  for( int n=0; n<np; n++ ) fill[n] = nptr[n];
+  for( int e=0; e<ne; e++ )
+    for( int i=0; i<6; i++ ) { int n = enodes[6*e+i]; nel[fill[n]++] = e; }
+  int* mark = (int*)malloc( (size_t)np * sizeof(int) );
+  for( int n=0; n<np; n++ ) mark[n] = -1;
+  int* nb = (int*)malloc( 4096 * sizeof(int) );
+  int64_t total;
+  for( int eq=0; eq<=neq; eq++ ) ptr[eq] = 0;
+  /* pass over nodes: the neighbour list of a node, then one row per equation of the node */
+  for( int n=0; n<np; n++ )
+  {
+    int cnt = 0;
+    for( int64_t q=nptr[n]; q<nptr[n+1]; q++ )
+    {
+      const int* nd = enodes + 6 * nel[q];
+      for( int i=0; i<6; i++ )
+        if( mark[nd[i]] != n && cnt < 4096 ) { mark[nd[i]] = n; nb[cnt++] = nd[i]; }
+    }
+    int ncols = 0;
+    for( int k=0; k<cnt; k++ )
+      for( int v=0; v<3; v++ ) if( eqno[3*nb[k]+v] >= 0 ) ncols++;
+    for( int v=0; v<3; v++ )
+    {
+      int row = eqno[3*n+v];
+      if( row < 0 ) continue;
+      ptr[row+1] = ncols;
+    }
+  }
+  for( int eq=0; eq<neq; eq++ ) ptr[eq+1] += ptr[eq];
+  total = ptr[neq];
+  if( idx )
+  {
+    for( int n=0; n<np; n++ ) mark[n] = -1;
+    for( int n=0; n<np; n++ )
+    {
+      int cnt = 0;
+      for( int64_t q=nptr[n]; q<nptr[n+1]; q++ )
+      {
+        const int* nd = enodes + 6 * nel[q];
+        for( int i=0; i<6; i++ )
+          if( mark[nd[i]] != n && cnt < 4096 ) { mark[nd[i]] = n; nb[cnt++] = nd[i]; }
+      }
+      for( int v=0; v<3; v++ )
+      {
+        int row = eqno[3*n+v];
+        if( row < 0 ) continue;
+        int64_t o = ptr[row];
+        idx[o++] = row;
+        for( int k=0; k<cnt; k++ )
+          for( int w=0; w<3; w++ )
+          {
+            int col = eqno[3*nb[k]+w];
+            if( col >= 0 && col != row ) idx[o++] = col;
+          }
+      }
+    }
+  }
+  free( nptr ); free( nel ); free( fill ); free( mark ); free( nb );
+  return total;
+}

@@ -103,6 +103,14 @@ void orc_friction(int np, int ne_region, const int* region_nodes, const int* reg
                   const double* V, const double* S, const double* z, double hmin, double g,
                   double* cf);
 
+/* CRS pattern of the equations of six-node triangles in the layout of
+ * EQS::SetIndexMat (IndexMat.cpp:91-342): diagonal first, then the equations of
+ * every node of every element that holds the row's node, first seen first
+ * (elements in list order, nodes in element order, U V S per node).  eqno: 3
+ * per node (-1: none).  ptr (neq + 1) is always filled; idx only when non-NULL.
+ * Returns the entry count. */
+int64_t orc_pattern(int np, int ne, const int* enodes, const int* eqno, int neq, int64_t* ptr, int* idx);
+
 /* discharge through the control sections (MODEL::Continuity, Contin.cpp:43-170):
  * control line elements in file order, 3 Gauss points each; section of element t
  * is seg_section[t] (1-based); Qx, Qy: nsect sums */

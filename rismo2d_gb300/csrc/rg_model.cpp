@@ -24,6 +24,7 @@
 #include "../../include/rg300_sim.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -661,32 +662,94 @@ static rg_status set_eqno(rg_sim* s) {
   for (size_t k = 0; k < eq.size(); k++)
     if (eq[k] >= 0) eq[k] = ord[eq[k]];
   s->neq = neq;
-  // CRS pattern, diagonal first then first-seen columns (IndexMat.cpp:126-288)
-  std::vector<std::vector<int>> rows(neq);
+  // CRS pattern, diagonal first then first-seen columns (IndexMat.cpp:126-288).  The
+  // columns of a row are the equations of every node of every model element that holds
+  // the row's node, first seen first (elements in model order, nodes in element order,
+  // U V S per node), so all rows of one node share one neighbour list; each node's
+  // rows are built on the host threads from a node -> element list.
+  const int np = s->np;
+  std::vector<long long> nptr(np + 1, 0);
   for (size_t e = 0; e < nme; e++) {
     const int* nd;
     int nnd;
     elem_nodes(s, s->melems[e], &nd, &nnd);
-    for (int i = 0; i < nnd; i++)
+    for (int i = 0; i < nnd; i++) nptr[nd[i] + 1]++;
+  }
+  for (int n = 0; n < np; n++) nptr[n + 1] += nptr[n];
+  std::vector<int> nel(nptr[np]);
+  {
+    std::vector<long long> fill(nptr.begin(), nptr.end() - 1);
+    for (size_t e = 0; e < nme; e++) {
+      const int* nd;
+      int nnd;
+      elem_nodes(s, s->melems[e], &nd, &nnd);
+      for (int i = 0; i < nnd; i++) nel[fill[nd[i]]++] = (int)e;
+    }
+  }
+  constexpr int kMaxNb = 256;
+  // neighbour nodes of n in first-seen order; false if there are more than kMaxNb
+  auto neighbours = [&](int n, int* nb, int* cnt) -> bool {
+    int c = 0;
+    for (long long q = nptr[n]; q < nptr[n + 1]; q++) {
+      const int* nd;
+      int nnd;
+      elem_nodes(s, s->melems[nel[q]], &nd, &nnd);
+      for (int i = 0; i < nnd; i++) {
+        const int m2 = nd[i];
+        bool seen = false;
+        for (int t = 0; t < c; t++)
+          if (nb[t] == m2) {
+            seen = true;
+            break;
+          }
+        if (seen) continue;
+        if (c == kMaxNb) return false;
+        nb[c++] = m2;
+      }
+    }
+    *cnt = c;
+    return true;
+  };
+  s->width.assign(neq, 0);
+  std::atomic<int> overflow{0};
+  HostPool& pool = *s->pool;
+  pool.run(np, [&](long long b, long long e, int) {
+    int nb[kMaxNb], c = 0;
+    for (long long n = b; n < e; n++) {
+      if (nptr[n] == nptr[n + 1]) continue;
+      if (!neighbours((int)n, nb, &c)) {
+        overflow = 1;
+        return;
+      }
+      int cols = 0;
+      for (int t = 0; t < c; t++)
+        for (int l = 0; l < 3; l++) cols += eq[3 * nb[t] + l] >= 0;
+      for (int j = 0; j < 3; j++)
+        if (eq[3 * n + j] >= 0) s->width[eq[3 * n + j]] = cols;
+    }
+  });
+  if (overflow) return sfail(s, RG_ERR_ARG, "CRS pattern: a node has more than 256 neighbours");
+  std::vector<long long> rp(neq + 1, 0);
+  for (int i = 0; i < neq; i++) rp[i + 1] = rp[i] + s->width[i];
+  s->index.assign((size_t)rp[neq], 0);
+  pool.run(np, [&](long long b, long long e, int) {
+    int nb[kMaxNb], c = 0;
+    for (long long n = b; n < e; n++) {
+      if (nptr[n] == nptr[n + 1] || !neighbours((int)n, nb, &c)) continue;
       for (int j = 0; j < 3; j++) {
-        int row = eq[3 * nd[i] + j];
+        const int row = eq[3 * n + j];
         if (row < 0) continue;
-        std::vector<int>& r = rows[row];
-        if (r.empty()) r.push_back(row);
-        for (int k = 0; k < nnd; k++)
+        int* out = s->index.data() + rp[row];
+        int o = 0;
+        out[o++] = row;
+        for (int t = 0; t < c; t++)
           for (int l = 0; l < 3; l++) {
-            int col = eq[3 * nd[k] + l];
-            if (col < 0) continue;
-            if (std::find(r.begin(), r.end(), col) == r.end()) r.push_back(col);
+            const int col = eq[3 * nb[t] + l];
+            if (col >= 0 && col != row) out[o++] = col;
           }
       }
-  }
-  s->width.assign(neq, 0);
-  s->index.clear();
-  for (int i = 0; i < neq; i++) {
-    s->width[i] = (int)rows[i].size();
-    s->index.insert(s->index.end(), rows[i].begin(), rows[i].end());
-  }
+    }
+  });
   return RG_OK;
 }
 

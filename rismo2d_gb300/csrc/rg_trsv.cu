@@ -53,13 +53,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return ok != 0;
 }
 
-// global -> shared bulk copy completing on an mbarrier (16-byte aligned, size % 16 == 0)
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+// global -> shared bulk copy completing on an mbarrier (16-byte aligned, size % 16 == 0);
+// the image is read once per solve, so its lines are marked first to leave L2 and the
+// solution vector (read back for far sources) stays resident
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
   asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
           smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
       : "memory");
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
 }
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -79,6 +87,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
     if (++it > limit) return false;
   }
   return true;
+}
+
+// a stage wait that ran out: error bit 8, and (first failure only) the kernel tag and the
+// chunk, read by the host's device-error check
+__device__ __forceinline__ void wave_wait_failed(int* err, int tag, int chunk) {
+  if (atomicCAS(&err[1], 0, tag) == 0) {
+    err[2] = chunk;
+    err[3] = -1;
+  }
+  atomicOr(err, 8);
 }
 
 __device__ __forceinline__ void consumers_sync() {
@@ -152,13 +170,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid >= kConsumers) {
     // ---- producer ------------------------------------------------------------
     if (tid == kConsumers && nchunks > 0) {
+      const uint64_t pol = policy_evict_first();
       WaveChunk next = chunks[0];
       for (int k = 0; k < nchunks; k++) {
         const int s = k % nst;
         const WaveChunk ch = next;
         if (k + 1 < nchunks) next = chunks[k + 1];   // descriptor load overlaps the wait below
         if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
-          atomicOr(err, 8);
+          wave_wait_failed(err, LOWER ? 30 : 31, k);
           break;
         }
         if (*v_abort) break;
@@ -166,7 +185,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         *v_issued = k + 1;
         fence_proxy_async();   // earlier generic reads of the stage precede the async refill
         mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
-        bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s]);
+        bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
       }
     }
     return;
@@ -178,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int s = k % nst;
     const bool got = mbar_wait_bounded(&full[s], (unsigned)((k / nst) & 1));
     if (!__all_sync(0xffffffffu, got)) {   // warp-uniform: the row sums below shuffle across lanes
-      atomicOr(err, 8);
+      if (lane == 0) wave_wait_failed(err, LOWER ? 30 : 31, k);
       *v_abort = 1;
     } else {
       const WaveChunk ch = sdesc[s];

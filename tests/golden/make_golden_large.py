@@ -9,6 +9,7 @@ compact fixture under tests/golden/:
     <case>.npz
       steps, newton[k], krylov[k], step_s[k]      per time step k
       scales_k                                    ||B|| of every Newton iteration of step k
+      krylov_k, solve_s_k, assemble_s_k           its BiCGStab count, EQS::Solve and assembly seconds
       sample                                      node indices of the stored values
       U_k, V_k, S_k, z_k                          end-of-step values at those nodes
       dry_k                                       packed bits of NODE::kDry for ALL nodes
@@ -97,6 +98,8 @@ def run(case: str, nsteps: int, workdir: str, max_sample: int, seed: int) -> dic
         step_s.append(float(s["seconds"]))
         out[f"scales_{k}"] = np.asarray(s["scales"], np.float64)
         out[f"krylov_{k}"] = np.asarray(s["iters"], np.int32)
+        out[f"solve_s_{k}"] = np.asarray(s["solve_s"], np.float64)        # EQS::Solve wall time per iteration
+        out[f"assemble_s_{k}"] = np.asarray(s["assemble_s"], np.float64)  # assembly wall time per iteration
         for v in ("U", "V", "S", "z"):
             out[f"{v}_{k}"] = np.asarray(s[v])[sample]
         out[f"dry_{k}"] = np.packbits(((s["flag"] & DRY) != 0).astype(np.uint8))

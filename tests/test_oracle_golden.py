@@ -121,3 +121,15 @@ def test_meander_assembly_and_solve_bit_exact():
         rc, ILU = oracle.ilu0_factor(st["ptr"], st["index"], A)
         ok, X, its, _ = oracle.bicgstab(st["ptr"], st["index"], A, ILU, B)
         assert its == g["iters"][k] and np.array_equal(X, st["X"])
+
+
+@pytest.mark.parametrize("name", ["channel_tiny.npz", "channel_1000.npz", "meander_tiny.npz"])
+def test_oracle_pattern_matches_reference(name):
+    """The oracle's CRS pattern builder reproduces EQS::SetIndexMat's width and index
+    arrays bit for bit from the reference's own equation numbers and element list."""
+    g = golden_io.load(name)
+    st = golden_io.state(g, 0)
+    six = st["elem_nnd"] == 6
+    ptr, idx = oracle.pattern(len(st["x"]), st["elem_nodes"][six], st["eqno"], len(st["width"]))
+    assert np.array_equal(np.diff(ptr), st["width"])
+    assert np.array_equal(idx, st["index"])
