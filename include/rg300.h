@@ -113,6 +113,14 @@ rg_status rg_set_relax(rg_ctx* ctx, double relaxThdt_UV, double relaxThdt_H);
  * Jacobian. */
 rg_status rg_set_jacobian(rg_ctx* ctx, int friction_depth);
 
+/* Polling limit of the bounded device waits of the dependency-driven ILU(0)
+ * factorisation and triangular solves (0 restores the built-in 2^20 polls).
+ * A wait that runs out makes the call return RG_ERR_DEVICE_WAIT with the
+ * kernel, row and awaited row in rg_last_error; the context stays usable.  A
+ * short limit makes waits give up early (used to test that path).  No
+ * counterpart in the reference. */
+rg_status rg_set_wait_limit(rg_ctx* ctx, long long polls);
+
 /* Assemble the Newton system on the GPU (CRSMAT::Init + AssembleEqs_im,
  * CRSMat.cpp:206, Assemble.cpp:195).  Optional outputs (NULL to skip):
  * B (neq doubles) and the matrix values in the reference's packed layout, as

@@ -5,6 +5,8 @@
 #include "rg_internal.cuh"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -287,6 +289,24 @@ cudaError_t launch_update(rg_ctx* c, const rg_update_opts* o, double* stats) {
 // =============================================================================
 // C ABI
 
+// Host loops of the pattern set-up run on plain threads in contiguous blocks
+// (each block writes only its own outputs, so the results do not depend on the
+// thread count).
+template <class F>
+static void par_blocks(long long n, F&& fn) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int nt = (int)std::min<unsigned>(hw ? hw : 1, 16);
+  if (const char* e = getenv("RG_HOST_THREADS")) nt = std::max(1, std::min(64, atoi(e)));
+  if (nt <= 1 || n < 65536) {
+    fn(0ll, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; t++) th.emplace_back([&, t] { fn(n * t / nt, n * (t + 1) / nt); });
+  fn(0ll, n / nt);
+  for (std::thread& x : th) x.join();
+}
+
 extern "C" {
 
 const char* rg_version(void) { return "rg300 0.1 (sm_103a)"; }
@@ -353,8 +373,10 @@ rg_status rg_create(const rg_mesh* m, int precision, int device, rg_ctx** out) {
   TRY(cudaMemsetAsync(c->bckind.p, 0, np * sizeof(int), c->st));
   TRY(c->ks.alloc(1));
   TRY(cudaMemsetAsync(c->ks.p, 0, sizeof(KrylovScalars), c->st));
-  TRY(c->dev_err.alloc(4));
-  TRY(cudaMemsetAsync(c->dev_err.p, 0, 4 * sizeof(int), c->st));
+  // error word: [0] bits, [1] kernel tag, [2] row, [3] awaited row; [4..5] the polling
+  // limit of the bounded waits (int64, 0 = the built-in limit)
+  TRY(c->dev_err.alloc(6));
+  TRY(cudaMemsetAsync(c->dev_err.p, 0, 6 * sizeof(int), c->st));
   TRY(c->upd.alloc(16));
   TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
@@ -384,10 +406,17 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     rowptr[i + 1] = rowptr[i] + width[i];
   }
   const int nnz = rowptr[neq];
-  for (int i = 0; i < neq; i++) {
-    if (index[rowptr[i]] != i) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: diagonal must come first");
-    for (int q = rowptr[i]; q < rowptr[i + 1]; q++)
-      if (index[q] < 0 || index[q] >= neq) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: column out of range");
+  {
+    std::atomic<int> bad{0};
+    par_blocks(neq, [&](long long b, long long e) {
+      for (long long i = b; i < e; i++) {
+        if (index[rowptr[i]] != i) bad = 1;
+        for (int q = rowptr[i]; q < rowptr[i + 1]; q++)
+          if (index[q] < 0 || index[q] >= neq) bad = 2;
+      }
+    });
+    if (bad == 1) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: diagonal must come first");
+    if (bad == 2) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: column out of range");
   }
   for (int k = 0; k < 3 * c->np; k++)
     if (eqno[k] < -1 || eqno[k] >= neq) return rg_fail(c, RG_ERR_ARG, "rg_set_pattern: bad equation number");
@@ -403,7 +432,8 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
   // done once per pattern instead of once per entry and iteration)
   const int ne = c->ne;
   std::vector<int> erow((size_t)ne * RG_EQ, -1), slot((size_t)ne * RG_EQ * RG_EQ, -1);
-  for (int e = 0; e < ne; e++) {
+  par_blocks(ne, [&](long long e0, long long e1) {
+  for (long long e = e0; e < e1; e++) {
     const int nnd = c->h_ennd[e];
     const int* nd = &c->h_enodes[6 * (size_t)e];
     int eq[RG_EQ];
@@ -426,6 +456,7 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       }
     }
   }
+  });
   TRY(upload(c, c->erow, erow.data(), erow.size()));
   TRY(upload(c, c->slot, slot.data(), slot.size()));
 
@@ -447,16 +478,23 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     for (int i = 0; i < nnd; i++) used[nd[i]] |= 1ull << k;
     ncol = std::max(ncol, k + 1);
   }
+  // per colour: its region elements, then its boundary lines, each in element order
   std::vector<int> celem;
   c->color_ptr.assign(3 * (size_t)ncol, 0);
-  for (int k = 0; k < ncol; k++) {
-    c->color_ptr[3 * k] = (int)celem.size();
+  {
+    std::vector<int> cnt(2 * (size_t)ncol + 1, 0);
     for (int e = 0; e < ne; e++)
-      if (color[e] == k && !(c->h_eflag[e] & RG_E_BOUND)) celem.push_back(e);
-    c->color_ptr[3 * k + 1] = (int)celem.size();
+      if (color[e] >= 0) cnt[2 * color[e] + ((c->h_eflag[e] & RG_E_BOUND) ? 1 : 0) + 1]++;
+    for (int k = 0; k < 2 * ncol; k++) cnt[k + 1] += cnt[k];
+    celem.resize(cnt[2 * ncol]);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int e = 0; e < ne; e++)
-      if (color[e] == k && (c->h_eflag[e] & RG_E_BOUND)) celem.push_back(e);
-    c->color_ptr[3 * k + 2] = (int)celem.size();
+      if (color[e] >= 0) celem[fill[2 * color[e] + ((c->h_eflag[e] & RG_E_BOUND) ? 1 : 0)]++] = e;
+    for (int k = 0; k < ncol; k++) {
+      c->color_ptr[3 * k] = cnt[2 * k];
+      c->color_ptr[3 * k + 1] = cnt[2 * k + 1];
+      c->color_ptr[3 * k + 2] = cnt[2 * k + 2];
+    }
   }
   TRY(upload(c, c->color_elem, celem.data(), celem.size()));
 
@@ -470,34 +508,59 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       for (int p = c->color_ptr[3 * k]; p < c->color_ptr[3 * k + 1]; p++) areg.push_back(p);
       for (int p = c->color_ptr[3 * k + 1]; p < c->color_ptr[3 * k + 2]; p++) abnd.push_back(p);
     }
+    // per equation: its contributions (position * RG_EQ + local row) in assembly order
     std::vector<long long> gptr((size_t)nnz + 1, 0), rptr((size_t)neq + 1, 0);
     for (long long p = 0; p < nasm; p++) {
       const int e = celem[p];
       const int nr = (c->h_eflag[e] & RG_E_BOUND) ? 9 : RG_EQ;
-      const int* sl = &slot[(size_t)e * RG_EQ * RG_EQ];
       for (int r = 0; r < nr; r++) {
-        for (int cc = 0; cc < nr; cc++)
-          if (sl[r * RG_EQ + cc] >= 0) gptr[sl[r * RG_EQ + cc] + 1]++;
         const int row = erow[(size_t)e * RG_EQ + r];
         if (row >= 0) rptr[row + 1]++;
       }
     }
-    for (size_t q = 0; q < (size_t)nnz; q++) gptr[q + 1] += gptr[q];
     for (int r = 0; r < neq; r++) rptr[r + 1] += rptr[r];
-    std::vector<int> gsrc((size_t)gptr[nnz]), rsrc((size_t)rptr[neq]);
-    std::vector<long long> gfill(gptr.begin(), gptr.end() - 1), rfill(rptr.begin(), rptr.end() - 1);
-    for (long long p = 0; p < nasm; p++) {
-      const int e = celem[p];
-      const int nr = (c->h_eflag[e] & RG_E_BOUND) ? 9 : RG_EQ;
-      const int* sl = &slot[(size_t)e * RG_EQ * RG_EQ];
-      for (int r = 0; r < nr; r++) {
-        for (int cc = 0; cc < nr; cc++) {
-          const int q = sl[r * RG_EQ + cc];
-          if (q >= 0) gsrc[gfill[q]++] = (int)(p * RG_EQ * RG_EQ + r * RG_EQ + cc);
+    std::vector<int> rsrc((size_t)rptr[neq]);
+    {
+      std::vector<long long> rfill(rptr.begin(), rptr.end() - 1);
+      for (long long p = 0; p < nasm; p++) {
+        const int e = celem[p];
+        const int nr = (c->h_eflag[e] & RG_E_BOUND) ? 9 : RG_EQ;
+        for (int r = 0; r < nr; r++) {
+          const int row = erow[(size_t)e * RG_EQ + r];
+          if (row >= 0) rsrc[rfill[row]++] = (int)(p * RG_EQ + r);
         }
-        const int row = erow[(size_t)e * RG_EQ + r];
-        if (row >= 0) rsrc[rfill[row]++] = (int)(p * RG_EQ + r);
       }
+    }
+    // per CRS entry: its contributions in assembly order.  Every entry of row r is fed
+    // only by the contributions of row r, so rows are processed independently, each
+    // walking its own contributions in assembly order.
+    auto row_entries = [&](long long r, bool fill_pass, std::vector<int>* gsrc, long long* gfill) {
+      for (long long t = rptr[r]; t < rptr[r + 1]; t++) {
+        const long long p = rsrc[t] / RG_EQ;
+        const int lr = (int)(rsrc[t] % RG_EQ);
+        const int e = celem[p];
+        const int nr = (c->h_eflag[e] & RG_E_BOUND) ? 9 : RG_EQ;
+        const int* sl = &slot[((size_t)e * RG_EQ + lr) * RG_EQ];
+        for (int cc = 0; cc < nr; cc++) {
+          const int q = sl[cc];
+          if (q < 0) continue;
+          if (fill_pass)
+            (*gsrc)[gfill[q]++] = (int)(p * RG_EQ * RG_EQ + lr * RG_EQ + cc);
+          else
+            gptr[q + 1]++;
+        }
+      }
+    };
+    par_blocks(neq, [&](long long b, long long e) {
+      for (long long r = b; r < e; r++) row_entries(r, false, nullptr, nullptr);
+    });
+    for (size_t q = 0; q < (size_t)nnz; q++) gptr[q + 1] += gptr[q];
+    std::vector<int> gsrc((size_t)gptr[nnz]);
+    {
+      std::vector<long long> gfill(gptr.begin(), gptr.end() - 1);
+      par_blocks(neq, [&](long long b, long long e) {
+        for (long long r = b; r < e; r++) row_entries(r, true, &gsrc, gfill.data());
+      });
     }
     c->n_asm_reg = (int)areg.size();
     c->n_asm_bnd = (int)abnd.size();
@@ -518,26 +581,37 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
   }
 
   // ILU(0) schedule: L positions sorted by column; split L/U operands
-  std::vector<int> lsp(neq + 1, 0), lspos, Lptr(neq + 1, 0), Lcol, Lsrc, Uptr(neq + 1, 0), Ucol, Usrc;
-  std::vector<std::pair<int, int>> tmp;
+  std::vector<int> lsp(neq + 1, 0), Lptr(neq + 1, 0), Uptr(neq + 1, 0);
   for (int i = 0; i < neq; i++) {
-    tmp.clear();
+    int nl = 0, nu = 0;
     for (int q = rowptr[i] + 1; q < rowptr[i + 1]; q++) {
-      if (index[q] < i) {
-        tmp.push_back({index[q], q - rowptr[i]});
-        Lcol.push_back(index[q]);
-        Lsrc.push_back(q);
-      } else if (index[q] > i) {
-        Ucol.push_back(index[q]);
-        Usrc.push_back(q);
-      }
+      if (index[q] < i) nl++;
+      else if (index[q] > i) nu++;
     }
-    std::sort(tmp.begin(), tmp.end());
-    for (auto& p : tmp) lspos.push_back(p.second);
-    lsp[i + 1] = (int)lspos.size();
-    Lptr[i + 1] = (int)Lcol.size();
-    Uptr[i + 1] = (int)Ucol.size();
+    Lptr[i + 1] = Lptr[i] + nl;
+    Uptr[i + 1] = Uptr[i] + nu;
   }
+  lsp = Lptr;
+  std::vector<int> lspos(Lptr[neq]), Lcol(Lptr[neq]), Lsrc(Lptr[neq]), Ucol(Uptr[neq]), Usrc(Uptr[neq]);
+  par_blocks(neq, [&](long long b, long long e) {
+    std::vector<std::pair<int, int>> tmp;
+    for (long long i = b; i < e; i++) {
+      tmp.clear();
+      int l = Lptr[i], u = Uptr[i];
+      for (int q = rowptr[i] + 1; q < rowptr[i + 1]; q++) {
+        if (index[q] < i) {
+          tmp.push_back({index[q], q - rowptr[i]});
+          Lcol[l] = index[q];
+          Lsrc[l++] = q;
+        } else if (index[q] > i) {
+          Ucol[u] = index[q];
+          Usrc[u++] = q;
+        }
+      }
+      std::sort(tmp.begin(), tmp.end());
+      for (size_t k = 0; k < tmp.size(); k++) lspos[lsp[i] + k] = tmp[k].second;
+    }
+  });
   TRY(upload(c, c->lsort_ptr, lsp.data(), lsp.size()));
   TRY(upload(c, c->lsort_pos, lspos.data(), std::max<size_t>(lspos.size(), 1)));
   TRY(upload(c, c->Lptr, Lptr.data(), Lptr.size()));
@@ -582,10 +656,14 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     // rows per chunk: one per consumer thread group (RG_WAVE_ROWS lowers the cap, for tuning)
     int rows_cap = kWaveRows / lanes;
     if (const char* e = getenv("RG_WAVE_ROWS")) rows_cap = std::max(32, std::min(rows_cap, atoi(e)));
-    WaveLayout wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, kWavePin, stage_cap,
-                                      rows_cap, lanes);
-    WaveLayout wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, kWavePin, stage_cap,
-                                      rows_cap, lanes);
+    WaveLayout wl, wu;
+    std::thread tl([&] {
+      wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, kWavePin, stage_cap, rows_cap,
+                             lanes);
+    });
+    wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, kWavePin, stage_cap, rows_cap,
+                           lanes);
+    tl.join();
     for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {
       WaveLayout& w = *pr.first;
       WaveDev& d = *pr.second;
@@ -597,6 +675,7 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       TRY(upload(c, d.ent_dst, w.ent_dst.data(), std::max<size_t>(w.ent_dst.size(), 1)));
       TRY(upload(c, d.diag_src, w.diag_src.data(), std::max<size_t>(w.diag_src.size(), 1)));
       TRY(upload(c, d.diag_dst, w.diag_dst.data(), std::max<size_t>(w.diag_dst.size(), 1)));
+      TRY(upload(c, d.far_rows, w.far_rows.data(), std::max<size_t>(w.far_rows.size(), 1)));
       d.nchunks = (long long)w.chunks.size();
       d.nent = (long long)w.ent_src.size();
       d.ndiag = (long long)w.diag_src.size();
@@ -605,7 +684,9 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       d.depth = w.depth;
       d.ring_misses = w.ring_misses;
       d.max_chunk_bytes = 0;
-      for (const WaveChunk& ch : w.chunks) d.max_chunk_bytes = std::max(d.max_chunk_bytes, ch.img_bytes);
+      // stage bytes a chunk needs: its image, then its far values
+      for (const WaveChunk& ch : w.chunks)
+        d.max_chunk_bytes = std::max(d.max_chunk_bytes, std::max(ch.img_bytes, ch.far_off + ch.nfar * vtb));
       TRY(cudaStreamSynchronize(c->st));   // host images are freed at scope end
     }
     // a row too wide for one stage (never with P2 triangles: at most ~45 entries)
@@ -737,6 +818,14 @@ rg_status rg_set_relax(rg_ctx* c, double relaxThdt_UV, double relaxThdt_H) {
   if (!c) return RG_ERR_ARG;
   c->rUV = relaxThdt_UV;
   c->rH = relaxThdt_H;
+  return RG_OK;
+}
+
+rg_status rg_set_wait_limit(rg_ctx* c, long long polls) {
+  if (!c || polls < 0) return rg_fail(c, RG_ERR_ARG, "rg_set_wait_limit: negative limit");
+  TRY(cudaSetDevice(c->device));
+  TRY(cudaMemcpyAsync(c->dev_err.p + 4, &polls, sizeof(long long), cudaMemcpyHostToDevice, c->st));
+  TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
 }
 

@@ -67,7 +67,10 @@ struct WaveChunk {
   int pos0;            // level-order position of the chunk's first row
   int b_off;           // byte offsets inside the image: right-hand side, diagonal (U solve)
   int diag_off;
-  int pad;
+  int nfar;            // distinct sources outside the ring and the pinned slots
+  int far_base;        // their rows: far_rows[far_base, far_base + nfar)
+  int far_off;         // byte offset in the stage of their values (after the image)
+  int pad0, pad1;
 };
 constexpr int kWaveSlice = 32;      // rows per warp slice
 constexpr int kWaveThreads = 544;   // one CTA: 16 consumer warps + 1 producer warp
@@ -85,14 +88,16 @@ struct WaveLayout {
   std::vector<WaveChunk> chunks;
   std::vector<unsigned char> img_host;
   long long img_bytes = 0;
-  std::vector<int> order, bidx, ent_src, diag_src;
+  std::vector<int> order, bidx, ent_src, diag_src, far_rows;
   std::vector<long long> ent_dst, diag_dst;
   long long ring_misses = 0;
   int pinned = 0;
 };
 // ring: shared-memory ring slots; pin: fixed slots for sources read from
 // farther back than the ring reaches (src encoding: [0, ring) ring slot,
-// [ring, ring + pin) pinned slot, negative: -(row + 1) in global memory);
+// [ring, ring + pin) pinned slot, ring + pin + f: value f of the chunk's far
+// list, gathered from global memory into the chunk's stage before the chunk
+// is solved);
 // bidx[p]: element index (in units of the vector type) of the right-hand side
 // slot of level-order position p inside the image
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
@@ -113,7 +118,7 @@ struct KrylovScalars {
 struct WaveDev {
   DBuf<unsigned char> img;
   DBuf<WaveChunk> chunks;
-  DBuf<int> order, bidx, ent_src, diag_src;
+  DBuf<int> order, bidx, ent_src, diag_src, far_rows;
   DBuf<long long> ent_dst, diag_dst;
   long long nchunks = 0, nent = 0, ndiag = 0;
   int stage_bytes = 0, lanes = 1, depth = 0, max_chunk_bytes = 0;

@@ -83,14 +83,23 @@ __device__ void record_wait_failure(int* err, int tag, int row, int dep) {
   atomicOr(&err[0], kDevErrWait);
 }
 
+// the polling limit of the bounded waits: err[4..5] holds the context's limit
+// (rg_set_wait_limit; 0 = kSpinLimit)
+__device__ __forceinline__ long long spin_limit(const int* err) {
+  const long long v = *reinterpret_cast<const volatile long long*>(err + 4);
+  return v > 0 ? v : kSpinLimit;
+}
+
 template <class T>
 __device__ __forceinline__ T wait_value(const T* p, int* err, int tag, int row, int dep) {
   T v = ld_relaxed(p);
+  if (!is_sent(v)) return v;
+  const long long limit = spin_limit(err);
   long long it = 0;
   while (is_sent(v)) {
     ++it;
     if ((it & 1023) == 0 && ld_relaxed_i(err) != 0) return (T)0;   // another warp gave up
-    if (it > kSpinLimit) {
+    if (it > limit) {
       record_wait_failure(err, tag, row, dep);
       return (T)0;
     }
@@ -100,11 +109,13 @@ __device__ __forceinline__ T wait_value(const T* p, int* err, int tag, int row, 
 }
 
 __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err, int tag, int row, int dep) {
+  if (ld_acquire(flag) == epoch) return true;
+  const long long limit = spin_limit(err);
   long long it = 0;
   while (ld_acquire(flag) != epoch) {
     ++it;
     if ((it & 1023) == 0 && ld_relaxed_i(err) != 0) return false;
-    if (it > kSpinLimit) {
+    if (it > limit) {
       record_wait_failure(err, tag, row, dep);
       return false;
     }

@@ -25,6 +25,11 @@
 namespace {
 
 constexpr int kThreads = kWaveThreads;
+// the producer gathers a chunk's far values when it refills the chunk's stage, up to
+// kWaveMaxStages chunks before the consumers reach it: far sources (more than the
+// ring's reach, kWaveRing - kWaveRows positions, before their row) must lie in
+// chunks the consumers have finished by then
+static_assert(kWaveRing - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the far-value gather");
 constexpr long long kMbarSpin = 1ll << 26;
 constexpr long long kDrainSpin = 1ll << 16;
 
@@ -127,17 +132,19 @@ template <>
 __device__ __forceinline__ double fadd<double>(double a, double b) { return __dadd_rn(a, b); }
 
 // the solution value at source slot s: ring or pinned slot, or (FAR layouts
-// only) -(row + 1) for a row read back from global memory
+// only) s - RING - PIN in the chunk's far values, which the producer warp
+// gathered from global memory into the chunk's stage before the chunk started
 template <class VT, bool FAR>
-__device__ __forceinline__ VT source_value(const VT* vals, const VT* x, int s) {
-  if (FAR) return s >= 0 ? vals[s] : x[-s - 1];
+__device__ __forceinline__ VT source_value(const VT* vals, const VT* farv, int s) {
+  if (FAR) return s < kWaveRing + kWavePin ? vals[s] : farv[s - kWaveRing - kWavePin];
   return vals[s];
 }
 
 template <class VT, bool LOWER, int G, bool FAR>
 __global__ void __launch_bounds__(kThreads, 1)
     k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, const unsigned char* __restrict__ img,
-                VT* __restrict__ x, int stage_bytes, int* err, const KrylovScalars* ks) {
+                const int* __restrict__ far_rows, VT* __restrict__ x, int stage_bytes, int* err,
+                const KrylovScalars* ks) {
   if (ks && ks->conv != 0) return;
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int RING = kWaveRing, PIN = kWavePin, nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
@@ -155,8 +162,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ int s_abort;    // set by a consumer whose wait ran out (read after a barrier)
   const int tid = threadIdx.x;
   if (tid == 0) {
+    // a stage is full when its image has landed (the copy's transaction bytes) and,
+    // in FAR layouts, the producer warp has stored the chunk's far values (a second arrival)
     for (int s = 0; s < nst; s++) {
-      mbar_init(&full[s], 1);
+      mbar_init(&full[s], FAR ? 2 : 1);
       mbar_init(&empty[s], 1);
     }
     s_issued = 0;
@@ -168,24 +177,39 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int* v_abort = &s_abort;
 
   if (tid >= kConsumers) {
-    // ---- producer ------------------------------------------------------------
-    if (tid == kConsumers && nchunks > 0) {
+    // ---- producer warp ----------------------------------------------------------
+    // lane 0 streams the chunk images; in FAR layouts all lanes then gather the
+    // chunk's far values.  Those rows lie at least the ring's reach before the chunk,
+    // i.e. in chunks the consumers finished before releasing the stage being refilled
+    // (the empty-barrier wait orders their stores before these loads).
+    const int plane = tid - kConsumers;
+    if (nchunks > 0) {
       const uint64_t pol = policy_evict_first();
       WaveChunk next = chunks[0];
       for (int k = 0; k < nchunks; k++) {
         const int s = k % nst;
         const WaveChunk ch = next;
         if (k + 1 < nchunks) next = chunks[k + 1];   // descriptor load overlaps the wait below
-        if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
+        bool ok = true;
+        if (plane == 0 && k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
           wave_wait_failed(err, LOWER ? 30 : 31, k);
-          break;
+          ok = false;
         }
-        if (*v_abort) break;
-        sdesc[s] = ch;
-        *v_issued = k + 1;
-        fence_proxy_async();   // earlier generic reads of the stage precede the async refill
-        mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
-        bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
+        if (!__all_sync(0xffffffffu, ok && !*v_abort)) break;
+        unsigned char* stage = stage0 + s * (size_t)stage_bytes;
+        if (plane == 0) {
+          sdesc[s] = ch;
+          *v_issued = k + 1;
+          fence_proxy_async();   // earlier generic reads of the stage precede the async refill
+          mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
+          bulk_g2s(stage, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
+        }
+        if (FAR) {
+          VT* farv = reinterpret_cast<VT*>(stage + ch.far_off);
+          for (int f = plane; f < ch.nfar; f += 32) farv[f] = __ldcg(&x[far_rows[ch.far_base + f]]);
+          __syncwarp();
+          if (plane == 0) mbar_arrive(&full[s]);
+        }
       }
     }
     return;
@@ -202,6 +226,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
       const WaveChunk ch = sdesc[s];
       const unsigned char* st = stage0 + s * (size_t)stage_bytes;
+      const VT* farv = reinterpret_cast<const VT*>(st + ch.far_off);
       const int r = tid / G, g = tid & (G - 1);
       const bool valid = r < ch.nrows;
       int4 mt = make_int4(0, 0, 0, -1);   // row, entries, slice offset, pinned slot
@@ -226,7 +251,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             vq[q] = val[(t + q) * kV];
           }
 #pragma unroll
-          for (int q = 0; q < 8; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
+          for (int q = 0; q < 8; q++) xq[q] = source_value<VT, FAR>(vals, farv, sq[q]);
 #pragma unroll
           for (int q = 0; q < 8; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
         }
@@ -239,7 +264,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             vq[q] = val[(t + q) * kV];
           }
 #pragma unroll
-          for (int q = 0; q < 4; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
+          for (int q = 0; q < 4; q++) xq[q] = source_value<VT, FAR>(vals, farv, sq[q]);
 #pragma unroll
           for (int q = 0; q < 4; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
           t += 4;
@@ -247,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (; t < cnt; t++) {
           const int s0 = src[t * kS];
           const VT v0 = val[t * kV];
-          const VT x0 = source_value<VT, FAR>(vals, x, s0);
+          const VT x0 = source_value<VT, FAR>(vals, farv, s0);
           acc = (LOWER || G > 1) ? fadd(acc, fmul(v0, x0)) : fadd(acc, -fmul(v0, x0));
         }
       }
@@ -310,8 +335,9 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
     if (e != cudaSuccess) return e;
     attr_done[c->device] = (int)smem;
   }
-  k_trsv_wave<VT, LOWER, G, FAR><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p, x,
-                                                                      wd.stage_bytes, c->dev_err.p, ks);
+  k_trsv_wave<VT, LOWER, G, FAR><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p,
+                                                                      wd.far_rows.p, x, wd.stage_bytes, c->dev_err.p,
+                                                                      ks);
   return cudaGetLastError();
 }
 

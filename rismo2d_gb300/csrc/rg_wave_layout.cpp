@@ -57,6 +57,16 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   const long long stride = kWaveSlice * (4ll + vt_bytes);   // bytes per entry column of a slice
   // chunk image: meta[m] (int4) | b[m] (VT) | diag[m] (VT, U only) | slices, each part 16-aligned
   auto head_bytes = [&](long long m) { return a16(16 * m) + a16(vt_bytes * m) + (lower ? 0 : a16(vt_bytes * m)); };
+  // a source is read from the ring when it lies less than ring - rows_max positions
+  // before the reading row (then it is less than ring positions before the end of the
+  // reader's chunk, so its slot has not been reused)
+  const int reach = ring - rows_max;
+  auto in_ring = [&](int reader_pos, int j) { return reader_pos - pos[j] < reach; };
+  // sources outside the ring, per row (an upper bound of the far values a chunk stages)
+  std::vector<int> far_cnt(n, 0);
+  for (int i = 0; i < n; i++)
+    for (int q = ptr[i]; q < ptr[i + 1]; q++)
+      if (!in_ring(pos[i], dep[q])) far_cnt[i]++;
   std::vector<int> chunk_end(n);
   int p = 0;
   long long img_off = 0;
@@ -66,12 +76,14 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
     WaveChunk ch{};
     ch.pos0 = p;
     int m = 0;
-    long long ebytes = 0;
+    long long ebytes = 0, fbytes = 0;
     while (p + m < lend && m < rows_max) {
       // a new slice starts every rps rows; its width is set by its first (longest) row
       const long long add = (m % rps == 0) ? (long long)((kof(order[p + m]) + lanes - 1) / lanes) * stride : 0;
-      if (m > 0 && head_bytes(m + 1) + ebytes + add > stage_cap) break;
+      const long long fadd = (long long)far_cnt[order[p + m]] * vt_bytes;
+      if (m > 0 && a16(head_bytes(m + 1) + ebytes + add) + fbytes + fadd > stage_cap) break;
       ebytes += add;
+      fbytes += fadd;
       m++;
     }
     ch.nrows = m;
@@ -89,7 +101,7 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   for (int i = 0; i < n; i++)
     for (int q = ptr[i]; q < ptr[i + 1]; q++) {
       const int j = dep[q];
-      if (chunk_end[pos[i]] - 1 - pos[j] >= ring) far_reads[j]++;
+      if (!in_ring(pos[i], j)) far_reads[j]++;
     }
   std::vector<int> cand;
   for (int j = 0; j < n; j++)
@@ -102,8 +114,10 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   w.order = order;
   w.bidx.resize(n);
   std::vector<unsigned char> img((size_t)img_off, 0);
-  for (const WaveChunk& ch : w.chunks) {
-    const int cend = ch.pos0 + ch.nrows;
+  std::vector<int> far_slot(n, -1);   // slot of a row in the current chunk's far list
+  for (WaveChunk& ch : w.chunks) {
+    ch.far_base = (int)w.far_rows.size();
+    ch.far_off = (int)a16(ch.img_bytes);
     long long sbase = head_bytes(ch.nrows);   // byte offset of the current slice in the chunk
     int width = 0;
     for (int r = 0; r < ch.nrows; r++) {
@@ -127,20 +141,27 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
         const int j = dep[q];
         const int pj = pos[j];
         int src;
-        if (cend - 1 - pj < ring)
+        if (in_ring(pp, j)) {
           src = pj % ring;
-        else if (pin_slot[j] >= 0)
+        } else if (pin_slot[j] >= 0) {
           src = ring + pin_slot[j];
-        else
-          src = -(j + 1);
+        } else {
+          if (far_slot[j] < 0) {
+            far_slot[j] = (int)w.far_rows.size() - ch.far_base;
+            w.far_rows.push_back(j);
+          }
+          src = ring + pin + far_slot[j];
+        }
         const int lane = rs * lanes + e % lanes;
         const long long col = ch.img_off + sbase + (long long)(e / lanes) * stride;
         std::memcpy(&img[(size_t)(col + 4ll * lane)], &src, 4);
         w.ent_dst.push_back(col + 4ll * kWaveSlice + (long long)vt_bytes * lane);
         w.ent_src.push_back(src_pos[q]);
-        if (src < 0) w.ring_misses++;
+        if (src >= ring + pin) w.ring_misses++;
       }
     }
+    ch.nfar = (int)w.far_rows.size() - ch.far_base;
+    for (int f = ch.far_base; f < (int)w.far_rows.size(); f++) far_slot[w.far_rows[f]] = -1;
   }
   w.img_host.swap(img);
   return w;

@@ -8,9 +8,8 @@ meshes of the shapes its workloads name:
 * ``meander`` -- straight valley with a sinusoidal main channel cut into sloping
   flood plains; the channel is carved into the bed elevation, the mesh is a
   structured grid over the valley.
-* ``braided`` -- 20 km x 2 km braided river: a fractal bed from three octaves
-  of gradient noise, bars with steep banks between anabranches, extensive
-  dry areas.
+* ``braided`` -- 20 km x 2 km braided river: intersecting anabranches between
+  bars whose bed is three octaves of gradient noise; the bars start dry.
 
 Node and element layout follow the reference's region-file conventions
 (``GRID::InputRegion``, Grid.cpp:159-298): six-node triangles list the three
@@ -187,41 +186,52 @@ def braided_hydrograph(Q0: float = 500.0, Qpeak: float = 3000.0, duration: float
 
 
 def braided(nx: int = 4000, ny: int = 500, length: float = 20000.0, width: float = 2000.0,
-            valley_slope: float = 5.0e-4, relief: float = 2.0, octaves: int = 3,
-            cell_x: float = 1600.0, cell_y: float = 400.0, sharpness: float = 50.0,
-            wall: float = 0.05, wall_height: float = 4.0, depth0: float = 0.5, kst: float = 30.0,
-            vt: float = 0.5, seed: int = 5, Q0: float = 500.0) -> Mesh:
-    """Braided gravel-bed river: a wide valley floor with a fractal bed.
+            valley_slope: float = 5.0e-4, anabranches: int = 5, branch_width=(80.0, 160.0),
+            branch_depth: float = 3.0, bar_rise: float = 1.0, relief: float = 2.0, octaves: int = 3,
+            cell_x: float = 1600.0, cell_y: float = 400.0, bed_relief: float = 0.3, depth0: float = 0.5,
+            kst: float = 30.0, vt: float = 0.5, seed: int = 5, Q0: float = 500.0) -> Mesh:
+    """Braided river: intersecting anabranches between bars on a fractal bed.
 
-    Bed = valley slope + gradient noise of ``octaves`` octaves (lattice cells
-    and amplitudes halve per octave; cells elongated along the valley like bars
-    and anabranches), sharpened as relief * tanh(sharpness * n) / tanh(sharpness)
-    of the noise n scaled to [-1, 1], so that bars rise from the anabranches
-    with steep banks (the default 50 makes the bank a step of about one
-    element: the reference's Newton iteration, whose Jacobian holds the
-    friction coefficient fixed and which clamps the bed under nodes shallower
-    than the dry limit, stalls near 1e-5 on wide shallow fringes and reaches
-    1e-8 in 25-30 iterations with steep banks), + valley walls ``wall_height`` high over the outer
-    ``wall`` fraction of the width on both sides.  The initial water surface
-    is a plane ``depth0`` above the valley axis, parallel to the valley: the
-    bars above it start dry, so wetting and drying is extensive.  Defaults:
-    20 km x 2 km, 4,000,000 six-node triangles, 8,009,001 nodes (5 m x 4 m
-    quads), bars up to 2 m above and anabranches down to 2 m below the axis.
+    ``anabranches`` sinuous channels (seeded amplitudes, wavelengths and phases,
+    widths in ``branch_width``) wander across the valley and cross each other;
+    their beds lie ``branch_depth`` below the valley line with a gradient-noise
+    roughness of +-``bed_relief``.  Between them the bars rise ``bar_rise`` to
+    ``bar_rise + relief`` above the valley line: gradient noise of ``octaves``
+    octaves (lattice cells and amplitudes halve per octave, cells elongated
+    along the valley), scaled to [0, 1] times ``relief``.  Banks are steps
+    between neighbouring nodes, as in ``meander``: the reference's Newton
+    iteration (Jacobian with the friction coefficient held fixed, bed clamped
+    under nodes shallower than the dry limit) stalls on wide shallow fringes,
+    which a smooth fractal bed under a shallow sheet of water produces.
+    The initial water surface lies ``depth0`` above the valley line, so the
+    bars start dry and flood as the hydrograph rises.  Defaults: 20 km x 2 km,
+    4,000,000 six-node triangles, 8,009,001 nodes (5 m x 4 m quads).
     """
     rng = np.random.default_rng(seed)
     ii, jj, els, inlet, outlet = _strip(nx, ny)
     x = length * ii / (2 * nx)
     y = width * jj / (2 * ny)
     valley = valley_slope * (length - x)
+    # bars: fractal relief scaled to [0, 1]
     noise = np.zeros_like(x)
     amp = 1.0
     for k in range(octaves):
         noise += amp * perlin(x, y, cell_x / 2 ** k, cell_y / 2 ** k, rng)
         amp *= 0.5
-    noise /= max(1e-12, float(np.max(np.abs(noise))))
-    bed = relief * (np.tanh(sharpness * noise) / np.tanh(sharpness) if sharpness > 0 else noise)
-    edge = np.minimum(y, width - y) < wall * width
-    z = valley + bed + np.where(edge, wall_height, 0.0)
+    lo, hi = float(np.min(noise)), float(np.max(noise))
+    bars = bar_rise + relief * (noise - lo) / max(1e-12, hi - lo)
+    # anabranch beds: a finer noise field of +-bed_relief
+    fine = perlin(x, y, cell_x / 4, cell_y / 4, rng)
+    fine *= bed_relief / max(1e-12, float(np.max(np.abs(fine))))
+    inside = np.zeros(x.shape, bool)
+    for _ in range(anabranches):
+        a = rng.uniform(0.2, 0.4) * width
+        lam = rng.uniform(2500.0, 6000.0)
+        phase = rng.uniform(0.0, 2.0 * np.pi)
+        w = rng.uniform(*branch_width)
+        yc = 0.5 * width + a * np.sin(2.0 * np.pi * x / lam + phase)
+        inside |= np.abs(y - yc) <= 0.5 * w
+    z = valley + np.where(inside, -branch_depth + fine, bars)
     S0 = np.maximum(valley + depth0, z)
     return Mesh(x=x.astype(np.float64), y=y.astype(np.float64), z=z, elems=els,
                 elem_type=np.ones(els.shape[0], np.int32), lines={1: inlet, 2: outlet}, S0=S0,

@@ -88,14 +88,30 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
   const long long stride = 32ll * (4 + vtb);
   for (int pass = 0; pass < 2; pass++) {
     std::vector<VT> ringv(ring + pin, (VT)NAN), x(n, (VT)NAN);
-    int written = 0;
+    std::vector<int> chunk_of(n, -1);
+    int written = 0, kchunk = -1;
     for (const WaveChunk& ch : w.chunks) {
+      kchunk++;
       CHECK(ch.img_off % 16 == 0 && ch.img_bytes % 16 == 0, "image alignment");
       CHECK(ch.b_off % 16 == 0 && ch.diag_off % 16 == 0, "part alignment");
       CHECK(ch.img_bytes <= stage_cap || ch.nrows == 1, "stage capacity %d > %d", ch.img_bytes, stage_cap);
       CHECK(ch.nrows >= 1 && ch.nrows <= rows_max, "rows per chunk");
       CHECK(ch.pos0 == written, "chunk positions contiguous");
       const unsigned char* st = &img[ch.img_off];
+      // the producer warp's gather of the chunk's far values (rows finished in earlier chunks)
+      CHECK(ch.far_off % 16 == 0 && ch.far_off >= ch.img_bytes, "far values after the image");
+      CHECK(ch.nrows == 1 || ch.far_off + (long long)ch.nfar * vtb <= stage_cap, "far values inside the stage");
+      CHECK(ch.far_base >= 0 && ch.far_base + ch.nfar <= (int)w.far_rows.size(), "far list range");
+      std::vector<VT> farv(ch.nfar);
+      for (int f = 0; f < ch.nfar; f++) {
+        const int j = w.far_rows[ch.far_base + f];
+        CHECK(j >= 0 && j < n && !std::isnan((double)x[j]), "far source %d not solved before its chunk", j);
+        // with the library's ring the producer gathers a chunk's far values up to
+        // kWaveMaxStages chunks ahead: their rows must be that much older
+        if (ring == kWaveRing)
+          CHECK(chunk_of[j] <= kchunk - kWaveMaxStages, "far source %d too recent for the gather", j);
+        farv[f] = x[j];
+      }
       for (int rr = 0; rr < ch.nrows; rr++) {
         int r = pass == 0 ? rr : ch.nrows - 1 - rr;
         int meta[4];
@@ -114,8 +130,8 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
           int src;
           std::memcpy(&src, st + meta[2] + (e / lanes) * stride + 4 * lane, 4);
           std::memcpy(&v, st + meta[2] + (e / lanes) * stride + 128 + (size_t)vtb * lane, sizeof(VT));
-          CHECK(src < ring + pin, "source slot out of range");
-          VT xv = src >= 0 ? ringv[src] : x[-src - 1];
+          CHECK(src >= 0 && src < ring + pin + ch.nfar, "source slot out of range");
+          VT xv = src < ring + pin ? ringv[src] : farv[src - ring - pin];
           VT prod = v * xv;
           part[g] = (lower || lanes > 1) ? part[g] + prod : part[g] - prod;
         }
@@ -137,6 +153,7 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
           ringv[meta[3]] = xi;
         }
         x[meta[0]] = xi;
+        chunk_of[meta[0]] = kchunk;
       }
       written += ch.nrows;
     }

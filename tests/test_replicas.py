@@ -49,7 +49,7 @@ def test_reference_arm_under_torchrun_rank0_only():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(REPO, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1"]
+           "--impl", "reference", "--workload", "meander200k", "--gpus", "2", "--steps", "1", "--warmup", "1"]
     out = subprocess.run(cmd, cwd=REPO, capture_output=True, text=True, timeout=900)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
