@@ -2,14 +2,16 @@
 """Seconds per shallow-water time step on one GB300, Newton iterated to 1e-8.
 
 Default workload (the metric's configuration, synthetic and seeded): the
-braided river of rismo2d_gb300.meshgen.braided -- 20 km x 2 km valley, fractal
-bed from three octaves of gradient noise with steep-banked bars (+-2 m),
-4,000,000 six-node triangles / 8,009,001 nodes, Manning n = 1/30, constant eddy
-viscosity 0.5 m^2/s (the k-epsilon closure is not built), no sediment.
-Unsteady, dt = 20 s, theta = 1, flood hydrograph Q(t) = 500 + 2500 sin^2(pi t /
-86400) m^3/s at the inlet, outlet level fixed, dry/rewet method 2 every 10
-Newton iterations (about 60% of the nodes start dry).  Every time step runs
-Newton until the scaled residual ||B_k|| / ||B_0|| <= 1e-8.
+braided river of rismo2d_gb300.meshgen.braided -- 20 km x 2 km valley, five
+intersecting sinuous anabranches (80-160 m wide, bed 3 m below the valley line
+with +-0.3 m gradient-noise roughness) between bars whose bed is three octaves
+of gradient noise 1 to 3 m above the valley line, 4,000,000 six-node triangles
+/ 8,009,001 nodes, Manning n = 1/30, constant eddy viscosity 0.5 m^2/s (the
+k-epsilon closure is not built), no sediment.  Unsteady, dt = 20 s, theta = 1,
+flood hydrograph Q(t) = 500 + 2500 sin^2(pi t / 86400) m^3/s at the inlet,
+outlet level fixed, dry/rewet method 2 every 10 Newton iterations (71% of the
+nodes start dry on the bars).  Every time step runs Newton until the scaled
+residual ||B_k|| / ||B_0|| <= 1e-8.
 `--workload meander200k` selects the 200,028-triangle meander (dt = 10 s).
 
 A "step" is one such time step.  Headline arm (`value`): the mixed-precision
@@ -70,9 +72,9 @@ def workloads():
             train_hyd=lambda m: meshgen.braided_hydrograph(Q0=400.0, Qpeak=2400.0, duration=64800.0,
                                                            S=m.meta["S_in"]),
             dt=20.0, train_steps=8,
-            desc=("braided river 20 km x 2 km, 4,000,000 P2 triangles (8,009,001 nodes), fractal steep-banked "
-                  "bed (3 octaves, +-2 m), unsteady dt=20 s, Q(t)=500+2500 sin^2(pi t/86400), dry/rewet on, "
-                  "Newton to ||B||/||B0||<=1e-8")),
+            desc=("braided river 20 km x 2 km, 4,000,000 P2 triangles (8,009,001 nodes), 5 anabranches between "
+                  "fractal bars (3 octaves, 2 m relief), unsteady dt=20 s, Q(t)=500+2500 sin^2(pi t/86400), "
+                  "dry/rewet on, Newton to ||B||/||B0||<=1e-8")),
         "meander200k": dict(
             mesh=lambda: meshgen.meander(),
             hyd=lambda m: meshgen.sin2_hydrograph(),

@@ -121,6 +121,16 @@ rg_status rg_set_jacobian(rg_ctx* ctx, int friction_depth);
  * counterpart in the reference. */
 rg_status rg_set_wait_limit(rg_ctx* ctx, long long polls);
 
+/* Mixed precision only: equations of nodes with depth S - z below `depth`
+ * (near-dry nodes) are eliminated in FP64 in the ILU(0) factorisation -- their
+ * multipliers and pivots computed in double from the FP32 pivot rows, then
+ * stored in FP32 like every factor entry.  Default for a mixed-precision
+ * context: 10 hmin (five times the dry limit when hmin is half of it); 0 turns
+ * it off.  The zero-pivot repair path (rare) factors in FP32.  No counterpart
+ * in the reference, whose factorisation rounds every entry to its float
+ * matrix type (Preco_ilu0.cpp:160-185). */
+rg_status rg_set_fp64_pivots(rg_ctx* ctx, double depth);
+
 /* Assemble the Newton system on the GPU (CRSMAT::Init + AssembleEqs_im,
  * CRSMat.cpp:206, Assemble.cpp:195).  Optional outputs (NULL to skip):
  * B (neq doubles) and the matrix values in the reference's packed layout, as

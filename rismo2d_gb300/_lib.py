@@ -28,7 +28,7 @@ PREC_MIXED = 2
 
 # every symbol the public header declares (checked by the CPU test suite)
 EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pattern", "rg_set_boundary",
-           "rg_set_state", "rg_get_state", "rg_set_relax", "rg_set_jacobian", "rg_set_wait_limit", "rg_assemble", "rg_load_system", "rg_scale",
+           "rg_set_state", "rg_get_state", "rg_set_relax", "rg_set_jacobian", "rg_set_wait_limit", "rg_set_fp64_pivots", "rg_assemble", "rg_load_system", "rg_scale",
            "rg_ilu0_factor", "rg_ilu0_apply", "rg_spmv", "rg_bicgstab", "rg_solve", "rg_set_update_lists",
            "rg_newton_update", "rg_set_friction", "rg_friction", "rg_continuity", "rg_get_timings",
            "rg_sim_create", "rg_sim_destroy", "rg_sim_last_error", "rg_sim_set_state", "rg_sim_get_state",
@@ -145,6 +145,9 @@ class Context:
         out = [np.zeros(self.np) for _ in range(4)]
         self._check(self.lib.rg_get_state(self.ptr, *[p(a) for a in out]), "rg_get_state")
         return dict(zip(["U", "V", "S", "z"], out))
+
+    def set_fp64_pivots(self, depth: float):
+        self._check(self.lib.rg_set_fp64_pivots(self.ptr, C.c_double(depth)), "rg_set_fp64_pivots")
 
     def set_wait_limit(self, polls: int):
         self._check(self.lib.rg_set_wait_limit(self.ptr, C.c_longlong(polls)), "rg_set_wait_limit")

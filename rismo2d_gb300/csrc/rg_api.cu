@@ -348,6 +348,7 @@ rg_status rg_create(const rg_mesh* m, int precision, int device, rg_ctx** out) {
   c->ne = m->ne;
   c->g = m->g;
   c->hmin = m->hmin;
+  if (precision == RG_PREC_MIXED) c->fp64_pivot_depth = 10.0 * m->hmin;   // near-dry rows factor in FP64
   c->vk = m->vk;
   TRY(upload(c, c->x, m->x, m->np));
   TRY(upload(c, c->y, m->y, m->np));
@@ -818,6 +819,12 @@ rg_status rg_set_relax(rg_ctx* c, double relaxThdt_UV, double relaxThdt_H) {
   if (!c) return RG_ERR_ARG;
   c->rUV = relaxThdt_UV;
   c->rH = relaxThdt_H;
+  return RG_OK;
+}
+
+rg_status rg_set_fp64_pivots(rg_ctx* c, double depth) {
+  if (!c || !(depth >= 0.0)) return rg_fail(c, RG_ERR_ARG, "rg_set_fp64_pivots: depth must be >= 0");
+  c->fp64_pivot_depth = depth;
   return RG_OK;
 }
 

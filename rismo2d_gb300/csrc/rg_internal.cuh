@@ -138,6 +138,7 @@ struct rg_ctx {
   int np = 0, ne = 0;
   double g = 9.81, hmin = 0.0, vk = 0.0, rUV = 0.0, rH = 0.0;
   int jac_friction = 0;       // rg_set_jacobian: depth derivative of the friction coefficient
+  double fp64_pivot_depth = 0.0;   // rg_set_fp64_pivots: rows shallower than this factor in FP64 (mixed)
   DBuf<double> x, y, evt;
   DBuf<int> enodes, ennd, eflag;
   std::vector<int> h_enodes, h_ennd, h_eflag, h_region_nodes;
@@ -220,6 +221,7 @@ struct rg_ctx {
   DBuf<long long> fmap_off;          // per sorted L entry: offset into fmap
   DBuf<int> lsort_col;               // per sorted L entry: its column (the pivot row)
   DBuf<short> fmap;                  // fill map (position in the row, -1 = dropped)
+  DBuf<unsigned char> fp64row;       // per equation: near-dry row, eliminated in FP64 (mixed)
   int use_wave = 1;
   int use_level_factor = 1;
   int n_repair_fallbacks = 0, n_factor_calls = 0;
@@ -278,6 +280,7 @@ cudaError_t launch_scale(rg_ctx* c, double* scale_host);
 cudaError_t launch_factor(rg_ctx* c);
 cudaError_t launch_factor_level(rg_ctx* c);
 cudaError_t launch_build_fmap(rg_ctx* c);
+cudaError_t launch_near_dry_rows(rg_ctx* c);
 cudaError_t launch_split(rg_ctx* c);
 cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r);
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x);

@@ -465,6 +465,10 @@ __global__ void k_build_fmap(int n, const int* __restrict__ rowptr, const int* _
 // level-scheduled ILU(0) with the fill map: per row, the pivots and pivot rows
 // of all its L entries are fetched in one parallel batch into shared memory,
 // then the eliminations run in column order from shared memory
+//
+// Rows flagged in fp64row (FP32 factors only: the rows of near-dry nodes in the
+// mixed precision path) are eliminated in FP64 -- the row, its multipliers and its
+// pivot in double, from the FP32 pivot rows -- and stored in FP32 like the others.
 template <class MT, int WARPS, int STAGE>
 __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const int* __restrict__ lev_ptr,
                                                               const int* __restrict__ lev_rows,
@@ -475,7 +479,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
                                                               const int* __restrict__ lsort_pos,
                                                               const int* __restrict__ lsort_col,
                                                               const long long* __restrict__ fmap_off,
-                                                              const short* __restrict__ fmap, int* err) {
+                                                              const short* __restrict__ fmap, int* err,
+                                                              const unsigned char* __restrict__ fp64row) {
   namespace cg = cooperative_groups;
   cg::grid_group grid = cg::this_grid();
   __shared__ MT sval[WARPS][RG_MAXW];
@@ -485,6 +490,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
   __shared__ int srow[WARPS][RG_MAXW];         // first U-side entry of the pivot row
   __shared__ MT stage[WARPS][STAGE];
   __shared__ short smap[WARPS][STAGE];
+  __shared__ double svd[sizeof(MT) == 4 ? WARPS : 1][RG_MAXW];   // FP64 working row of a flagged row
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * WARPS + wib, nw = gridDim.x * WARPS;
   for (int l = 0; l < nlev; l++) {
@@ -530,6 +536,31 @@ __global__ void __launch_bounds__(WARPS * 32) k_factor_level2(int nlev, const in
         }
       }
       __syncwarp();
+      if (sizeof(MT) == 4 && fp64row && fp64row[i]) {
+        // near-dry row: the elimination in FP64 (same order, same fill map)
+        double* rw = svd[sizeof(MT) == 4 ? wib : 0];
+        for (int j = lane; j < w; j += 32) rw[j] = (double)sval[wib][j];
+        __syncwarp();
+        for (int p = 0; p < nl; p++) {
+          const int pp = spos[wib][p];
+          const double factor = -rw[pp] / (double)spiv[wib][p];
+          __syncwarp();
+          if (lane == 0) rw[pp] = factor;
+          const int dst = sbeg[wib][p], cnt = sbeg[wib][p + 1] - dst;
+          const int bk = srow[wib][p];
+          const long long mo = fmap_off[q0 + p];
+          for (int t = lane; t < cnt; t += 32) {
+            const int pos = staged ? smap[wib][dst + t] : fmap[mo + t];
+            const double u = staged ? (double)stage[wib][dst + t] : (double)__ldcg(&LU[bk + t]);
+            if (pos >= 0) rw[pos] = __dadd_rn(rw[pos], __dmul_rn(factor, u));
+          }
+          __syncwarp();
+        }
+        if (lane == 0 && fabs(rw[0]) < 1.0e-20) atomicOr(&err[0], 16);   // needs the repair path
+        for (int j = lane; j < w; j += 32) __stcg(&LU[b + j], (MT)rw[j]);
+        __syncwarp();
+        continue;
+      }
       for (int p = 0; p < nl; p++) {
         const int pp = spos[wib][p];
         const MT factor = -sval[wib][pp] / spiv[wib][p];
@@ -888,8 +919,36 @@ static cudaError_t launch_factor_level2_t(rg_ctx* c, const MT* A, MT* LU) {
   const long long* fo = c->fmap_off.p;
   const short* fm = c->fmap.p;
   int* err = c->dev_err.p;
-  void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &lscol, &fo, &fm, &err};
+  const unsigned char* f64 = nullptr;
+  if (sizeof(MT) == 4 && c->prec == RG_PREC_MIXED && c->fp64_pivot_depth > 0.0 && c->S.p && c->z.p) {
+    cudaError_t e2 = launch_near_dry_rows(c);
+    if (e2 != cudaSuccess) return e2;
+    f64 = c->fp64row.p;
+  }
+  void* args[] = {&nlev, &lp, &lr, &rp, &cl, &A, &LU, &lsp, &lspos, &lscol, &fo, &fm, &err, &f64};
   return cudaLaunchCooperativeKernel((void*)k_factor_level2<MT, WARPS, STAGE>, blocks, WARPS * 32, args, 0, rg_counted(c));
+}
+
+// rows of the nodes shallower than the context's FP64-pivot depth (rg_set_fp64_pivots)
+__global__ void k_near_dry_rows(int np, const double* __restrict__ S, const double* __restrict__ z,
+                                const int* __restrict__ eqno, double depth, unsigned char* __restrict__ flag, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
+    const bool shallow = S[k] - z[k] < depth;
+    for (int j = 0; j < 3; j++) {
+      const int e = eqno[3 * k + j];
+      if (e >= 0 && e < n) flag[e] = shallow ? 1 : 0;
+    }
+  }
+}
+
+cudaError_t launch_near_dry_rows(rg_ctx* c) {
+  cudaError_t e = c->fp64row.alloc((size_t)c->neq);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(c->fp64row.p, 0, (size_t)c->neq, c->st);
+  if (e != cudaSuccess) return e;
+  k_near_dry_rows<<<grid_for(c, c->np, 256), 256, 0, rg_counted(c)>>>(c->np, c->S.p, c->z.p, c->eqno.p,
+                                                                      c->fp64_pivot_depth, c->fp64row.p, c->neq);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_build_fmap(rg_ctx* c) {
