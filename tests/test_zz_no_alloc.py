@@ -57,3 +57,21 @@ def test_noalloc_rejects_oversized_system():
     assert rc == lib.RG_ERR_ARG
     assert b"exceed the fixed scratch" in ctx.lib.rg_last_error(ctx.ptr)
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_overlapping_vectors():
+    """The solves fill x before they read b: an x that overlaps b is refused."""
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    st = golden_io.state(golden_io.load("channel_tiny.npz"), 0)
+    ctx = golden_io.gpu_context(st, lib.PREC_MIXED)
+    ctx.assemble(want_A=False)
+    ctx.scale()
+    ctx.ilu0_factor()
+    v = torch.zeros(2 * ctx.neq, dtype=torch.float64, device="cuda:0")
+    p0 = v.data_ptr()
+    rc = ctx.lib.rg_ilu0_apply_dev_noalloc(ctx.ptr, C.c_void_p(p0), C.c_void_p(p0 + 8 * (ctx.neq // 2)))
+    assert rc == lib.RG_ERR_ARG
+    assert b"overlap" in ctx.lib.rg_last_error(ctx.ptr)
+    ctx.close()
