@@ -155,6 +155,11 @@ rg_status rg_ilu0_factor(rg_ctx* ctx, float* LU32_out, double* LU64_out);
 /* PRECO_ILU0::Solve (Preco_ilu0.cpp:497-980) of a host vector. */
 rg_status rg_ilu0_apply(rg_ctx* ctx, const double* B, double* X);
 
+/* PRECO_ILU0::Solve in FP32, for mixed-precision contexts: the preconditioner
+ * of the mixed path's inner BiCGStab (FP32 factors and vectors, summation
+ * order free), on host float vectors.  RG_ERR_ARG for other precisions. */
+rg_status rg_ilu0_apply_f32(rg_ctx* ctx, const float* B, float* X);
+
 /* ILU(0) preconditioner applied to a DEVICE vector without allocating:
  * x_dev = M^-1 b_dev with the resident factors.  It has no counterpart in the
  * reference.  It is meant for callers that must not allocate during a solve: a

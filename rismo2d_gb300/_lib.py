@@ -29,7 +29,7 @@ PREC_MIXED = 2
 # every symbol the public header declares (checked by the CPU test suite)
 EXPORTS = ["rg_create", "rg_destroy", "rg_last_error", "rg_version", "rg_set_pattern", "rg_set_boundary",
            "rg_set_state", "rg_get_state", "rg_set_relax", "rg_set_jacobian", "rg_set_wait_limit", "rg_set_fp64_pivots", "rg_assemble", "rg_load_system", "rg_scale",
-           "rg_ilu0_factor", "rg_ilu0_apply", "rg_spmv", "rg_bicgstab", "rg_solve", "rg_set_update_lists",
+           "rg_ilu0_factor", "rg_ilu0_apply", "rg_ilu0_apply_f32", "rg_spmv", "rg_bicgstab", "rg_solve", "rg_set_update_lists",
            "rg_newton_update", "rg_set_friction", "rg_friction", "rg_continuity", "rg_get_timings",
            "rg_sim_create", "rg_sim_destroy", "rg_sim_last_error", "rg_sim_set_state", "rg_sim_get_state",
            "rg_sim_step", "rg_sim_prepare_iteration", "rg_sim_get_numbering", "rg_sim_get_pattern",
@@ -191,6 +191,12 @@ class Context:
         b = np.ascontiguousarray(b, np.float64)
         x = np.zeros(self.neq)
         self._check(self.lib.rg_ilu0_apply(self.ptr, p(b), p(x)), "rg_ilu0_apply")
+        return x
+
+    def ilu0_apply_f32(self, b):
+        b = np.ascontiguousarray(b, np.float32)
+        x = np.zeros(self.neq, np.float32)
+        self._check(self.lib.rg_ilu0_apply_f32(self.ptr, p(b), p(x)), "rg_ilu0_apply_f32")
         return x
 
     def spmv(self, x):

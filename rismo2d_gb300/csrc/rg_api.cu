@@ -657,13 +657,17 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     // rows per chunk: one per consumer thread group (RG_WAVE_ROWS lowers the cap, for tuning)
     int rows_cap = kWaveRows / lanes;
     if (const char* e = getenv("RG_WAVE_ROWS")) rows_cap = std::max(32, std::min(rows_cap, atoi(e)));
+    // FP32 solves of the mixed path: far entries summed by helper blocks (split layouts;
+    // RG_WAVE_SPLIT=0 keeps them in the images, read from global memory)
+    bool split = c->prec == RG_PREC_MIXED && lanes == 1;
+    if (const char* e = getenv("RG_WAVE_SPLIT")) split = split && atoi(e) != 0;
     WaveLayout wl, wu;
     std::thread tl([&] {
       wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, kWavePin, stage_cap, rows_cap,
-                             lanes);
+                             lanes, split);
     });
     wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, kWavePin, stage_cap, rows_cap,
-                           lanes);
+                           lanes, split);
     tl.join();
     for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {
       WaveLayout& w = *pr.first;
@@ -676,7 +680,19 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       TRY(upload(c, d.ent_dst, w.ent_dst.data(), std::max<size_t>(w.ent_dst.size(), 1)));
       TRY(upload(c, d.diag_src, w.diag_src.data(), std::max<size_t>(w.diag_src.size(), 1)));
       TRY(upload(c, d.diag_dst, w.diag_dst.data(), std::max<size_t>(w.diag_dst.size(), 1)));
-      TRY(upload(c, d.far_rows, w.far_rows.data(), std::max<size_t>(w.far_rows.size(), 1)));
+      d.split = split;
+      d.nfar = (long long)w.far_src.size();
+      if (split) {
+        TRY(upload(c, d.far_ptr, w.far_ptr.data(), w.far_ptr.size()));
+        TRY(upload(c, d.far_src, w.far_src.data(), std::max<size_t>(w.far_src.size(), 1)));
+        TRY(upload(c, d.far_vsrc, w.far_vsrc.data(), std::max<size_t>(w.far_vsrc.size(), 1)));
+        TRY(d.far_val.alloc(std::max<size_t>(w.far_src.size(), 1) * sizeof(float)));
+        TRY(d.chunk_ready.alloc(std::max<size_t>(w.chunks.size(), 1)));
+        TRY(cudaMemsetAsync(d.chunk_ready.p, 0, d.chunk_ready.bytes(), c->st));
+        TRY(d.progress.alloc(1));
+        TRY(cudaMemsetAsync(d.progress.p, 0, sizeof(unsigned long long), c->st));
+        d.epoch = 0;
+      }
       d.nchunks = (long long)w.chunks.size();
       d.nent = (long long)w.ent_src.size();
       d.ndiag = (long long)w.diag_src.size();
@@ -685,9 +701,8 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
       d.depth = w.depth;
       d.ring_misses = w.ring_misses;
       d.max_chunk_bytes = 0;
-      // stage bytes a chunk needs: its image, then its far values
       for (const WaveChunk& ch : w.chunks)
-        d.max_chunk_bytes = std::max(d.max_chunk_bytes, std::max(ch.img_bytes, ch.far_off + ch.nfar * vtb));
+        d.max_chunk_bytes = std::max(d.max_chunk_bytes, ch.img_bytes);
       TRY(cudaStreamSynchronize(c->st));   // host images are freed at scope end
     }
     // a row too wide for one stage (never with P2 triangles: at most ~45 entries)
@@ -962,6 +977,19 @@ rg_status rg_ilu0_factor(rg_ctx* c, float* LU32_out, double* LU64_out) {
   }
   c->have_factor = true;
   if (LU32_out || LU64_out) return copy_out_system(c, nullptr, LU32_out, LU64_out, true);
+  return RG_OK;
+}
+
+rg_status rg_ilu0_apply_f32(rg_ctx* c, const float* B, float* X) {
+  if (!c || !c->have_factor || !B || !X) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply_f32: no factors");
+  if (c->prec != RG_PREC_MIXED) return rg_fail(c, RG_ERR_ARG, "rg_ilu0_apply_f32: mixed-precision contexts only");
+  TRY(cudaSetDevice(c->device));
+  TRY(rg_copy(c, c->f_pi.p, B, c->neq * sizeof(float), cudaMemcpyHostToDevice));
+  TRY(launch_ilu_apply_f(c, c->f_pi.p, c->f_w.p, c->f_yi.p));
+  rg_status s = check_device_error(c);
+  if (s != RG_OK) return s;
+  TRY(rg_copy(c, X, c->f_yi.p, c->neq * sizeof(float), cudaMemcpyDeviceToHost));
+  TRY(cudaStreamSynchronize(c->st));
   return RG_OK;
 }
 

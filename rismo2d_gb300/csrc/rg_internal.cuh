@@ -67,10 +67,8 @@ struct WaveChunk {
   int pos0;            // level-order position of the chunk's first row
   int b_off;           // byte offsets inside the image: right-hand side, diagonal (U solve)
   int diag_off;
-  int nfar;            // distinct sources outside the ring and the pinned slots
-  int far_base;        // their rows: far_rows[far_base, far_base + nfar)
-  int far_off;         // byte offset in the stage of their values (after the image)
-  int pad0, pad1;
+  int far_dep;         // split layouts: the last chunk holding a far source of this chunk (-1: none)
+  int pad0, pad1, pad2, pad3;
 };
 constexpr int kWaveSlice = 32;      // rows per warp slice
 constexpr int kWaveThreads = 544;   // one CTA: 16 consumer warps + 1 producer warp
@@ -88,21 +86,29 @@ struct WaveLayout {
   std::vector<WaveChunk> chunks;
   std::vector<unsigned char> img_host;
   long long img_bytes = 0;
-  std::vector<int> order, bidx, ent_src, diag_src, far_rows;
+  std::vector<int> order, bidx, ent_src, diag_src;
   std::vector<long long> ent_dst, diag_dst;
+  // split layouts: the far entries of the row at level-order position p are
+  // far_src[far_ptr[p], far_ptr[p + 1]) (source rows), their values packed into
+  // the far value array from factor positions far_vsrc
+  std::vector<long long> far_ptr;
+  std::vector<int> far_src, far_vsrc;
   long long ring_misses = 0;
   int pinned = 0;
 };
 // ring: shared-memory ring slots; pin: fixed slots for sources read from
 // farther back than the ring reaches (src encoding: [0, ring) ring slot,
-// [ring, ring + pin) pinned slot, ring + pin + f: value f of the chunk's far
-// list, gathered from global memory into the chunk's stage before the chunk
-// is solved);
+// [ring, ring + pin) pinned slot, negative: -(row + 1) read from global
+// memory).  split = true (FP32 solves, whose summation order is free): the
+// entries whose source lies outside the ring and the pinned slots leave the
+// chunk image for the far lists, summed into the right-hand side by helper
+// blocks before the chunk is solved;
 // bidx[p]: element index (in units of the vector type) of the right-hand side
 // slot of level-order position p inside the image
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
                              const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
-                             int vt_bytes, int ring, int pin, int stage_cap, int rows_max, int lanes);
+                             int vt_bytes, int ring, int pin, int stage_cap, int rows_max, int lanes,
+                             bool split = false);
 // threads per row of the wavefront solves: one, i.e. the reference's summation
 // order (bit-identical for double vectors); 2 or 4 split long rows
 constexpr int kWaveLanes64 = 1, kWaveLanes32 = 1;
@@ -118,7 +124,17 @@ struct KrylovScalars {
 struct WaveDev {
   DBuf<unsigned char> img;
   DBuf<WaveChunk> chunks;
-  DBuf<int> order, bidx, ent_src, diag_src, far_rows;
+  DBuf<int> order, bidx, ent_src, diag_src;
+  // split layouts: far lists, their values, and the per-chunk flags and progress
+  // word of the helper blocks
+  DBuf<long long> far_ptr;
+  DBuf<int> far_src, far_vsrc;
+  DBuf<unsigned char> far_val;
+  DBuf<int> chunk_ready;
+  DBuf<unsigned long long> progress;
+  bool split = false;
+  long long nfar = 0;
+  unsigned epoch = 0;
   DBuf<long long> ent_dst, diag_dst;
   long long nchunks = 0, nent = 0, ndiag = 0;
   int stage_bytes = 0, lanes = 1, depth = 0, max_chunk_bytes = 0;
@@ -285,6 +301,7 @@ cudaError_t launch_split(rg_ctx* c);
 cudaError_t launch_spmv_d(rg_ctx* c, const double* x, double* r);
 cudaError_t launch_ilu_apply_d(rg_ctx* c, const double* b, double* x);
 cudaError_t launch_ilu_apply_w(rg_ctx* c, const double* b, double* w, double* x);
+cudaError_t launch_ilu_apply_f(rg_ctx* c, const float* b, float* w, float* y);
 rg_status   run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, double* acc);
 cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void* y, const KrylovScalars* ks);
 cudaError_t launch_wave_pack(rg_ctx* c);

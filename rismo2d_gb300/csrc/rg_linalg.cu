@@ -1179,6 +1179,16 @@ rg_status run_bicgstab(rg_ctx* c, int maxIter, double maxDiff, int* iters, doubl
   return st;
 }
 
+// y = M^-1 b on float vectors with the FP32 factors of a mixed-precision context: the
+// inner solve of the mixed BiCGStab (wavefront kernels, or the dependency-driven ones)
+cudaError_t launch_ilu_apply_f(rg_ctx* c, const float* b, float* w, float* y) {
+  if (c->use_wave) return launch_wave_solve(c, false, b, w, y, nullptr);
+  int nb = grid_for(c, c->neq, 256);
+  k_fill_sentinel<float><<<nb, 256, 0, rg_counted(c)>>>(w, c->neq);
+  k_fill_sentinel<float><<<nb, 256, 0, rg_counted(c)>>>(y, c->neq);
+  return ilu_apply_t<float, float>(c, c->Lv32.p, c->Uv32.p, c->Dv32.p, b, w, y, nullptr);
+}
+
 // y = M^-1 b on double vectors with a caller-chosen intermediate w (n values):
 // the same kernels as launch_ilu_apply_d, which uses the context's own vector
 cudaError_t launch_ilu_apply_w(rg_ctx* c, const double* b, double* w, double* x) {

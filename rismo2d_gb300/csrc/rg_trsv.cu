@@ -15,7 +15,18 @@
 //     decides per entry where its source is (else it is read from global memory);
 //   * one consumer thread per row; chunks are separated by a named barrier.
 // Levels too large for a stage are split into consecutive chunks (rows of one
-// level do not depend on each other).  All waits are bounded.
+// level do not depend on each other).
+//
+// FP32 solves (whose summation order is free) use split layouts: entries whose
+// source lies outside the ring and the pinned slots -- about a fifth of them
+// on the 4M-triangle river -- are not in the images.  The same cooperative
+// launch then holds helper blocks: a helper takes a future chunk once the
+// wavefront block has published (progress word) that the chunk's far sources
+// are solved, sums the chunk's far contributions into its right-hand side in
+// the image and flags the chunk; the producer stages a chunk only after its
+// flag.  Far sources lie at least the ring's reach (~31 chunks) behind, so the
+// helpers work ahead of the wavefront and the far reads leave its critical
+// path.  All waits are bounded.
 
 #include "rg_internal.cuh"
 
@@ -25,12 +36,13 @@
 namespace {
 
 constexpr int kThreads = kWaveThreads;
-// the producer gathers a chunk's far values when it refills the chunk's stage, up to
-// kWaveMaxStages chunks before the consumers reach it: far sources (more than the
-// ring's reach, kWaveRing - kWaveRows positions, before their row) must lie in
-// chunks the consumers have finished by then
-static_assert(kWaveRing - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the far-value gather");
+// a chunk's far sources lie at least the ring's reach (kWaveRing - kWaveRows
+// positions, so more than kWaveMaxStages chunks) before it: the wavefront block
+// has finished them before its producer stages the chunk, so a helper can always
+// complete a chunk the producer waits for
+static_assert(kWaveRing - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helper blocks");
 constexpr long long kMbarSpin = 1ll << 26;
+constexpr long long kFlagSpin = 1ll << 24;   // polls of a global flag (~10 s at L2 latency)
 constexpr long long kDrainSpin = 1ll << 16;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
@@ -104,6 +116,16 @@ __device__ __forceinline__ void wave_wait_failed(int* err, int tag, int chunk) {
   atomicOr(err, 8);
 }
 
+// bounded wait that also gives up when the producer has aborted (checked every 1024 polls)
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, unsigned parity, volatile int* abort_flag) {
+  long long it = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++it > kMbarSpin) return false;
+    if ((it & 1023) == 0 && *abort_flag) return false;
+  }
+  return true;
+}
+
 __device__ __forceinline__ void consumers_sync() {
   asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");
 }
@@ -132,20 +154,99 @@ template <>
 __device__ __forceinline__ double fadd<double>(double a, double b) { return __dadd_rn(a, b); }
 
 // the solution value at source slot s: ring or pinned slot, or (FAR layouts
-// only) s - RING - PIN in the chunk's far values, which the producer warp
-// gathered from global memory into the chunk's stage before the chunk started
+// only) -(row + 1) for a row read back from global memory
 template <class VT, bool FAR>
-__device__ __forceinline__ VT source_value(const VT* vals, const VT* farv, int s) {
-  if (FAR) return s < kWaveRing + kWavePin ? vals[s] : farv[s - kWaveRing - kWavePin];
+__device__ __forceinline__ VT source_value(const VT* vals, const VT* x, int s) {
+  if (FAR) return s >= 0 ? vals[s] : __ldcg(&x[-s - 1]);
   return vals[s];
 }
 
-template <class VT, bool LOWER, int G, bool FAR>
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// generic-proxy writes to global memory before async-proxy (TMA) reads of it
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Helper block of a split solve: for its chunks k = h, h + H, ... (h = block - 1,
+// H = helpers) with far entries, wait until the wavefront block has solved the
+// chunk's far sources, add the far contributions of every row (one thread per
+// row) to the row's right-hand side in the image, and flag the chunk.
+template <class VT, bool LOWER>
+__device__ void wave_helper(int nchunks, const WaveChunk* __restrict__ chunks, unsigned char* img,
+                            const VT* __restrict__ x, int* err, const long long* __restrict__ far_ptr,
+                            const int* __restrict__ far_src, const VT* __restrict__ far_val,
+                            const int* __restrict__ bidx, int* chunk_ready, const unsigned long long* progress,
+                            unsigned epoch) {
+  __shared__ int s_go;
+  const int H = gridDim.x - 1;
+  VT* bimg = reinterpret_cast<VT*>(img);
+  for (int k = blockIdx.x - 1; k < nchunks; k += H) {
+    const WaveChunk ch = chunks[k];
+    if (ch.far_dep < 0) continue;
+    if (threadIdx.x == 0) {
+      const unsigned long long need = ((unsigned long long)epoch << 32) | (unsigned long long)(ch.far_dep + 1);
+      long long it = 0;
+      int go = 1;
+      while (ld_acquire_u64(progress) < need) {
+        if ((++it & 1023) == 0 && *reinterpret_cast<volatile int*>(err) != 0) {
+          go = 0;
+          break;
+        }
+        if (it > kFlagSpin) {
+          wave_wait_failed(err, LOWER ? 32 : 33, k);
+          go = 0;
+          break;
+        }
+      }
+      s_go = go;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    for (int r = threadIdx.x; r < ch.nrows; r += blockDim.x) {
+      const int p = ch.pos0 + r;
+      const long long e0 = far_ptr[p], e1 = far_ptr[p + 1];
+      if (e0 == e1) continue;
+      VT sum = 0;
+      for (long long e = e0; e < e1; e++) sum += far_val[e] * __ldcg(&x[far_src[e]]);
+      const int bi = bidx[p];
+      bimg[bi] = LOWER ? bimg[bi] + sum : bimg[bi] - sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      fence_proxy_async_global();
+      st_release_s32(&chunk_ready[k], (int)epoch);
+    }
+  }
+}
+
+template <class VT, bool LOWER, int G, bool FAR, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1)
-    k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, const unsigned char* __restrict__ img,
-                const int* __restrict__ far_rows, VT* __restrict__ x, int stage_bytes, int* err,
-                const KrylovScalars* ks) {
+    k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, unsigned char* img, VT* __restrict__ x,
+                int stage_bytes, int* err, const KrylovScalars* ks, const long long* __restrict__ far_ptr,
+                const int* __restrict__ far_src, const VT* __restrict__ far_val, const int* __restrict__ bidx,
+                int* chunk_ready, unsigned long long* progress, unsigned epoch) {
   if (ks && ks->conv != 0) return;
+  if (SPLIT && blockIdx.x > 0) {
+    wave_helper<VT, LOWER>(nchunks, chunks, img, x, err, far_ptr, far_src, far_val, bidx, chunk_ready, progress,
+                           epoch);
+    return;
+  }
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int RING = kWaveRing, PIN = kWavePin, nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
   constexpr int kConsumers = kThreads - 32;
@@ -162,10 +263,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ int s_abort;    // set by a consumer whose wait ran out (read after a barrier)
   const int tid = threadIdx.x;
   if (tid == 0) {
-    // a stage is full when its image has landed (the copy's transaction bytes) and,
-    // in FAR layouts, the producer warp has stored the chunk's far values (a second arrival)
     for (int s = 0; s < nst; s++) {
-      mbar_init(&full[s], FAR ? 2 : 1);
+      mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     s_issued = 0;
@@ -177,39 +276,46 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int* v_abort = &s_abort;
 
   if (tid >= kConsumers) {
-    // ---- producer warp ----------------------------------------------------------
-    // lane 0 streams the chunk images; in FAR layouts all lanes then gather the
-    // chunk's far values.  Those rows lie at least the ring's reach before the chunk,
-    // i.e. in chunks the consumers finished before releasing the stage being refilled
-    // (the empty-barrier wait orders their stores before these loads).
-    const int plane = tid - kConsumers;
-    if (nchunks > 0) {
+    // ---- producer ------------------------------------------------------------
+    if (tid == kConsumers && nchunks > 0) {
       const uint64_t pol = policy_evict_first();
       WaveChunk next = chunks[0];
       for (int k = 0; k < nchunks; k++) {
         const int s = k % nst;
         const WaveChunk ch = next;
         if (k + 1 < nchunks) next = chunks[k + 1];   // descriptor load overlaps the wait below
-        bool ok = true;
-        if (plane == 0 && k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
+        if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
           wave_wait_failed(err, LOWER ? 30 : 31, k);
-          ok = false;
+          *v_abort = 1;
+          break;
         }
-        if (!__all_sync(0xffffffffu, ok && !*v_abort)) break;
-        unsigned char* stage = stage0 + s * (size_t)stage_bytes;
-        if (plane == 0) {
-          sdesc[s] = ch;
-          *v_issued = k + 1;
-          fence_proxy_async();   // earlier generic reads of the stage precede the async refill
-          mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
-          bulk_g2s(stage, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
+        if (*v_abort) break;
+        if (SPLIT && ch.far_dep >= 0) {
+          // the helper's far sums must be in the image before it is staged
+          long long it = 0;
+          bool ok = true;
+          while (ld_acquire_s32(&chunk_ready[k]) != (int)epoch) {
+            if ((++it & 1023) == 0 && (*reinterpret_cast<volatile int*>(err) != 0 || *v_abort)) {
+              ok = false;
+              break;
+            }
+            if (it > kFlagSpin) {
+              wave_wait_failed(err, LOWER ? 34 : 35, k);
+              ok = false;
+              break;
+            }
+          }
+          if (!ok) {
+            *v_abort = 1;
+            break;
+          }
+          fence_proxy_async_global();
         }
-        if (FAR) {
-          VT* farv = reinterpret_cast<VT*>(stage + ch.far_off);
-          for (int f = plane; f < ch.nfar; f += 32) farv[f] = __ldcg(&x[far_rows[ch.far_base + f]]);
-          __syncwarp();
-          if (plane == 0) mbar_arrive(&full[s]);
-        }
+        sdesc[s] = ch;
+        *v_issued = k + 1;
+        fence_proxy_async();   // earlier generic reads of the stage precede the async refill
+        mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
+        bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
       }
     }
     return;
@@ -219,14 +325,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int lane = tid & 31;
   for (int k = 0; k < nchunks; k++) {
     const int s = k % nst;
-    const bool got = mbar_wait_bounded(&full[s], (unsigned)((k / nst) & 1));
+    const bool got = mbar_wait_abortable(&full[s], (unsigned)((k / nst) & 1), v_abort);
     if (!__all_sync(0xffffffffu, got)) {   // warp-uniform: the row sums below shuffle across lanes
       if (lane == 0) wave_wait_failed(err, LOWER ? 30 : 31, k);
       *v_abort = 1;
     } else {
       const WaveChunk ch = sdesc[s];
       const unsigned char* st = stage0 + s * (size_t)stage_bytes;
-      const VT* farv = reinterpret_cast<const VT*>(st + ch.far_off);
       const int r = tid / G, g = tid & (G - 1);
       const bool valid = r < ch.nrows;
       int4 mt = make_int4(0, 0, 0, -1);   // row, entries, slice offset, pinned slot
@@ -251,7 +356,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             vq[q] = val[(t + q) * kV];
           }
 #pragma unroll
-          for (int q = 0; q < 8; q++) xq[q] = source_value<VT, FAR>(vals, farv, sq[q]);
+          for (int q = 0; q < 8; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
 #pragma unroll
           for (int q = 0; q < 8; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
         }
@@ -264,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             vq[q] = val[(t + q) * kV];
           }
 #pragma unroll
-          for (int q = 0; q < 4; q++) xq[q] = source_value<VT, FAR>(vals, farv, sq[q]);
+          for (int q = 0; q < 4; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
 #pragma unroll
           for (int q = 0; q < 4; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
           t += 4;
@@ -272,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (; t < cnt; t++) {
           const int s0 = src[t * kS];
           const VT v0 = val[t * kV];
-          const VT x0 = source_value<VT, FAR>(vals, farv, s0);
+          const VT x0 = source_value<VT, FAR>(vals, x, s0);
           acc = (LOWER || G > 1) ? fadd(acc, fmul(v0, x0)) : fadd(acc, -fmul(v0, x0));
         }
       }
@@ -293,6 +398,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
     consumers_sync();                 // chunk k complete: its values are visible, its stage is free
+    // publish the progress for the helper blocks (x stores of the chunk precede it)
+    if (SPLIT && tid == 0) {
+      __threadfence();
+      st_release_u64(progress, ((unsigned long long)epoch << 32) | (unsigned long long)(k + 1));
+    }
     if (*v_abort) {
       // a copy never completed: stop, after giving the copies already started a bounded time to land
       if (tid == 0)
@@ -321,24 +431,60 @@ __global__ void k_pack_wave(int nent, const long long* __restrict__ ent_dst, con
   for (int q = t; q < ndiag; q += stride) *reinterpret_cast<VT*>(img + diag_dst[q]) = (VT)LU[diag_src[q]];
 }
 
+// factor values of the far entries (split layouts)
+template <class MT, class VT>
+__global__ void k_pack_far(long long nfar, const int* __restrict__ far_vsrc, const MT* __restrict__ LU,
+                           VT* __restrict__ far_val) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nfar; q += (long long)gridDim.x * blockDim.x)
+    far_val[q] = (VT)LU[far_vsrc[q]];
+}
+
 }  // namespace
 
 // ---- host side ----------------------------------------------------------------
 
-template <class VT, bool LOWER, int G, bool FAR>
+template <class VT, bool LOWER, int G, bool FAR, bool SPLIT>
 static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScalars* ks, size_t smem) {
   static int attr_done[kMaxDevices] = {0};   // per device: the attribute is a device property
+  static int blocks_dev[kMaxDevices] = {0};  // co-resident blocks of the split launch
   if (!device_slot_ok(c)) return cudaErrorInvalidDevice;
+  auto kern = k_trsv_wave<VT, LOWER, G, FAR, SPLIT>;
   if (attr_done[c->device] < (int)smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_trsv_wave<VT, LOWER, G, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr_done[c->device] = (int)smem;
+    blocks_dev[c->device] = 0;
   }
-  k_trsv_wave<VT, LOWER, G, FAR><<<1, kThreads, smem, rg_counted(c)>>>((int)wd.nchunks, wd.chunks.p, wd.img.p,
-                                                                      wd.far_rows.p, x, wd.stage_bytes, c->dev_err.p,
-                                                                      ks);
-  return cudaGetLastError();
+  int nchunks = (int)wd.nchunks;
+  const WaveChunk* chunks = wd.chunks.p;
+  unsigned char* img = wd.img.p;
+  int stage_bytes = wd.stage_bytes;
+  int* err = c->dev_err.p;
+  const long long* fptr = wd.far_ptr.p;
+  const int* fsrc = wd.far_src.p;
+  const VT* fval = reinterpret_cast<const VT*>(wd.far_val.p);
+  const int* bidx = wd.bidx.p;
+  int* ready = wd.chunk_ready.p;
+  unsigned long long* prog = wd.progress.p;
+  unsigned epoch = 0;
+  if (!SPLIT) {
+    kern<<<1, kThreads, smem, rg_counted(c)>>>(nchunks, chunks, img, x, stage_bytes, err, ks, fptr, fsrc, fval, bidx,
+                                               ready, prog, epoch);
+    return cudaGetLastError();
+  }
+  // one wavefront block and a helper block on every other SM, all co-resident
+  if (blocks_dev[c->device] == 0) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+    blocks_dev[c->device] = per_sm * c->num_sms;
+  }
+  int blocks = std::max(2, std::min(blocks_dev[c->device], c->num_sms));
+  epoch = ++wd.epoch;
+  void* args[] = {&nchunks, &chunks, &img, &x, &stage_bytes, &err, &ks, &fptr, &fsrc, &fval, &bidx, &ready, &prog,
+                  &epoch};
+  return cudaLaunchCooperativeKernel((void*)kern, blocks, kThreads, args, smem, rg_counted(c));
 }
 
 template <class VT, bool LOWER>
@@ -349,12 +495,19 @@ static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, con
   k_gather_lev<VT><<<nb, 256, 0, rg_counted(c)>>>(n, wd.order.p, wd.bidx.p, b, reinterpret_cast<VT*>(wd.img.p), ks);
   const int nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
   const size_t smem = (kWaveRing + kWavePin) * sizeof(VT) + (size_t)nst * (size_t)wd.stage_bytes;
+  if (wd.split) {
+    if (sizeof(VT) != 4 || wd.lanes != 1) return cudaErrorInvalidValue;   // split layouts: FP32, one lane per row
+    return launch_wave_k<VT, LOWER, 1, false, true>(c, wd, x, ks, smem);
+  }
   const bool far = wd.ring_misses > 0;
   if (sizeof(VT) == 8 || wd.lanes == 1)
-    return far ? launch_wave_k<VT, LOWER, 1, true>(c, wd, x, ks, smem) : launch_wave_k<VT, LOWER, 1, false>(c, wd, x, ks, smem);
+    return far ? launch_wave_k<VT, LOWER, 1, true, false>(c, wd, x, ks, smem)
+               : launch_wave_k<VT, LOWER, 1, false, false>(c, wd, x, ks, smem);
   if (wd.lanes == 2)
-    return far ? launch_wave_k<VT, LOWER, 2, true>(c, wd, x, ks, smem) : launch_wave_k<VT, LOWER, 2, false>(c, wd, x, ks, smem);
-  return far ? launch_wave_k<VT, LOWER, 4, true>(c, wd, x, ks, smem) : launch_wave_k<VT, LOWER, 4, false>(c, wd, x, ks, smem);
+    return far ? launch_wave_k<VT, LOWER, 2, true, false>(c, wd, x, ks, smem)
+               : launch_wave_k<VT, LOWER, 2, false, false>(c, wd, x, ks, smem);
+  return far ? launch_wave_k<VT, LOWER, 4, true, false>(c, wd, x, ks, smem)
+             : launch_wave_k<VT, LOWER, 4, false, false>(c, wd, x, ks, smem);
 }
 
 cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void* y, const KrylovScalars* ks) {
@@ -376,9 +529,14 @@ cudaError_t launch_wave_solve(rg_ctx* c, bool dbl, const void* b, void* w, void*
   return prof_end(c);
 }
 
-// pack the current factors into both images
+// pack the current factors into both images (and the far values of split layouts)
 cudaError_t launch_wave_pack(rg_ctx* c) {
   for (WaveDev* wd : {&c->waveL, &c->waveU}) {
+    if (wd->split && wd->nfar > 0) {
+      const int nbf = (int)std::min<long long>((wd->nfar + 255) / 256, (long long)c->num_sms * 8);
+      k_pack_far<float, float><<<nbf, 256, 0, rg_counted(c)>>>(wd->nfar, wd->far_vsrc.p, c->LU32.p,
+                                                                 reinterpret_cast<float*>(wd->far_val.p));
+    }
     int nb = (int)std::min<long long>((wd->nent + 255) / 256 + 1, (long long)c->num_sms * 8);
     if (c->prec == RG_PREC_FP64)
       k_pack_wave<double, double><<<nb, 256, 0, rg_counted(c)>>>((int)wd->nent, wd->ent_dst.p, wd->ent_src.p,

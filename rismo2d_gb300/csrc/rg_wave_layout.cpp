@@ -19,9 +19,15 @@
 // 32 / lanes rows): lane g of a row takes its entries g, g + lanes, ...; with
 // one lane per row the entries are summed in the factor's order, which is the
 // order of PRECO_ILU0::Solve (Preco_ilu0.cpp:517-530, 964-980).
+//
+// split = true: an entry whose source is neither in the ring nor pinned leaves
+// the image for the far lists of its row (far_ptr/far_src/far_vsrc, by
+// level-order position); each chunk records the last chunk holding one of its
+// far sources (far_dep).  Otherwise such an entry reads its source from global
+// memory (slot code -(row + 1)).
 WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vector<int>& dep,
                              const std::vector<int>& src_pos, const std::vector<int>& diag_pos, bool lower,
-                             int vt_bytes, int ring, int pin, int stage_cap, int rows_max, int lanes) {
+                             int vt_bytes, int ring, int pin, int stage_cap, int rows_max, int lanes, bool split) {
   WaveLayout w;
   w.n = n;
   const int rps = kWaveSlice / lanes;   // rows per warp slice
@@ -62,40 +68,6 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   // reader's chunk, so its slot has not been reused)
   const int reach = ring - rows_max;
   auto in_ring = [&](int reader_pos, int j) { return reader_pos - pos[j] < reach; };
-  // sources outside the ring, per row (an upper bound of the far values a chunk stages)
-  std::vector<int> far_cnt(n, 0);
-  for (int i = 0; i < n; i++)
-    for (int q = ptr[i]; q < ptr[i + 1]; q++)
-      if (!in_ring(pos[i], dep[q])) far_cnt[i]++;
-  std::vector<int> chunk_end(n);
-  int p = 0;
-  long long img_off = 0;
-  while (p < n) {
-    const int l = lev[order[p]];
-    const int lend = cnt[l + 1];
-    WaveChunk ch{};
-    ch.pos0 = p;
-    int m = 0;
-    long long ebytes = 0, fbytes = 0;
-    while (p + m < lend && m < rows_max) {
-      // a new slice starts every rps rows; its width is set by its first (longest) row
-      const long long add = (m % rps == 0) ? (long long)((kof(order[p + m]) + lanes - 1) / lanes) * stride : 0;
-      const long long fadd = (long long)far_cnt[order[p + m]] * vt_bytes;
-      if (m > 0 && a16(head_bytes(m + 1) + ebytes + add) + fbytes + fadd > stage_cap) break;
-      ebytes += add;
-      fbytes += fadd;
-      m++;
-    }
-    ch.nrows = m;
-    ch.b_off = (int)a16(16ll * m);
-    ch.diag_off = (int)(ch.b_off + a16((long long)vt_bytes * m));
-    ch.img_bytes = (int)(head_bytes(m) + ebytes);
-    ch.img_off = img_off;
-    img_off += ch.img_bytes;
-    for (int r = 0; r < m; r++) chunk_end[p + r] = p + m;
-    w.chunks.push_back(ch);
-    p += m;
-  }
   // sources outside the ring: pin the most-read ones in a fixed shared-memory table
   std::vector<int> far_reads(n, 0);
   for (int i = 0; i < n; i++)
@@ -110,14 +82,62 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   std::vector<int> pin_slot(n, -1);
   for (size_t k = 0; k < cand.size() && (int)k < pin; k++) pin_slot[cand[k]] = (int)k;
   w.pinned = (int)std::min<size_t>(cand.size(), (size_t)pin);
+  auto is_near = [&](int reader_pos, int j) { return in_ring(reader_pos, j) || pin_slot[j] >= 0; };
+  // entries a row keeps in the image: all of them, or (split) its near ones
+  std::vector<int> kimg(n);
+  for (int i = 0; i < n; i++) {
+    if (!split) {
+      kimg[i] = kof(i);
+      continue;
+    }
+    int k = 0;
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) k += is_near(pos[i], dep[q]);
+    kimg[i] = k;
+  }
+  // a slice's width: the widest row of its (up to rps) rows, counted to the end of the level
+  auto slice_width = [&](int p0, int lend) {
+    int wmax = 0;
+    for (int t = p0; t < std::min(p0 + rps, lend); t++) wmax = std::max(wmax, (kimg[order[t]] + lanes - 1) / lanes);
+    return wmax;
+  };
+  std::vector<int> chunk_end(n), chunk_of(n);
+  int p = 0;
+  long long img_off = 0;
+  while (p < n) {
+    const int l = lev[order[p]];
+    const int lend = cnt[l + 1];
+    WaveChunk ch{};
+    ch.pos0 = p;
+    ch.far_dep = -1;
+    int m = 0;
+    long long ebytes = 0;
+    while (p + m < lend && m < rows_max) {
+      // a new slice starts every rps rows
+      const long long add = (m % rps == 0) ? (long long)slice_width(p + m, lend) * stride : 0;
+      if (m > 0 && head_bytes(m + 1) + ebytes + add > stage_cap) break;
+      ebytes += add;
+      m++;
+    }
+    ch.nrows = m;
+    ch.b_off = (int)a16(16ll * m);
+    ch.diag_off = (int)(ch.b_off + a16((long long)vt_bytes * m));
+    ch.img_bytes = (int)(head_bytes(m) + ebytes);
+    ch.img_off = img_off;
+    img_off += ch.img_bytes;
+    for (int r = 0; r < m; r++) {
+      chunk_end[p + r] = p + m;
+      chunk_of[p + r] = (int)w.chunks.size();
+    }
+    w.chunks.push_back(ch);
+    p += m;
+  }
   w.img_bytes = img_off;
   w.order = order;
   w.bidx.resize(n);
   std::vector<unsigned char> img((size_t)img_off, 0);
-  std::vector<int> far_slot(n, -1);   // slot of a row in the current chunk's far list
+  if (split) w.far_ptr.assign(1, 0);
   for (WaveChunk& ch : w.chunks) {
-    ch.far_base = (int)w.far_rows.size();
-    ch.far_off = (int)a16(ch.img_bytes);
+    const int lend = cnt[lev[order[ch.pos0]] + 1];
     long long sbase = head_bytes(ch.nrows);   // byte offset of the current slice in the chunk
     int width = 0;
     for (int r = 0; r < ch.nrows; r++) {
@@ -126,18 +146,17 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
       const int rs = r % rps;   // row inside its slice
       if (rs == 0) {
         if (r > 0) sbase += (long long)width * stride;
-        width = (kof(i) + lanes - 1) / lanes;
+        width = slice_width(pp, lend);
       }
       w.bidx[pp] = (int)((ch.img_off + ch.b_off) / vt_bytes + r);
-      const int k = kof(i);
-      int mt[4] = {i, k, (int)sbase, pin_slot[i] >= 0 ? ring + pin_slot[i] : -1};
+      int mt[4] = {i, kimg[i], (int)sbase, pin_slot[i] >= 0 ? ring + pin_slot[i] : -1};
       std::memcpy(&img[(size_t)ch.img_off + 16 * (size_t)r], mt, 16);
       if (!lower) {
         w.diag_dst.push_back(ch.img_off + ch.diag_off + (long long)vt_bytes * r);
         w.diag_src.push_back(diag_pos[i]);
       }
-      for (int e = 0; e < k; e++) {
-        const int q = ptr[i] + e;
+      int e = 0;   // entry index inside the image
+      for (int q = ptr[i]; q < ptr[i + 1]; q++) {
         const int j = dep[q];
         const int pj = pos[j];
         int src;
@@ -146,22 +165,24 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
         } else if (pin_slot[j] >= 0) {
           src = ring + pin_slot[j];
         } else {
-          if (far_slot[j] < 0) {
-            far_slot[j] = (int)w.far_rows.size() - ch.far_base;
-            w.far_rows.push_back(j);
+          w.ring_misses++;
+          if (split) {
+            w.far_src.push_back(j);
+            w.far_vsrc.push_back(src_pos[q]);
+            ch.far_dep = std::max(ch.far_dep, chunk_of[pj]);
+            continue;
           }
-          src = ring + pin + far_slot[j];
+          src = -(j + 1);
         }
         const int lane = rs * lanes + e % lanes;
         const long long col = ch.img_off + sbase + (long long)(e / lanes) * stride;
         std::memcpy(&img[(size_t)(col + 4ll * lane)], &src, 4);
         w.ent_dst.push_back(col + 4ll * kWaveSlice + (long long)vt_bytes * lane);
         w.ent_src.push_back(src_pos[q]);
-        if (src >= ring + pin) w.ring_misses++;
+        e++;
       }
+      if (split) w.far_ptr.push_back((long long)w.far_src.size());
     }
-    ch.nfar = (int)w.far_rows.size() - ch.far_base;
-    for (int f = ch.far_base; f < (int)w.far_rows.size(); f++) far_slot[w.far_rows[f]] = -1;
   }
   w.img_host.swap(img);
   return w;

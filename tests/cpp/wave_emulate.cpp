@@ -26,8 +26,11 @@ static int fails = 0;
     }                                      \
   } while (0)
 
+static long long g_far_entries = 0;   // far entries over all split runs
+
 template <class VT>
-static void run(int n, int band, int seed, bool lower, int ring, int pin, int stage_cap, int lanes) {
+static void run(int n, int band, int seed, bool lower, int ring, int pin, int stage_cap, int lanes,
+                bool split = false) {
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> U(-1.0, 1.0);
   // random triangular structure within a band
@@ -56,7 +59,10 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
   const int vtb = sizeof(VT);
   const int rows_max = kWaveRows / lanes;
   const int rps = 32 / lanes;
-  WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, pin, stage_cap, rows_max, lanes);
+  WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, pin, stage_cap, rows_max, lanes,
+                                   split);
+  CHECK(!split || (long long)w.far_ptr.size() == (long long)n + 1, "far list per position");
+  g_far_entries += (long long)w.far_src.size();
   // pack values as the device kernel does
   std::vector<unsigned char> img = w.img_host;
   for (size_t q = 0; q < w.ent_dst.size(); q++) {
@@ -89,6 +95,7 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
   for (int pass = 0; pass < 2; pass++) {
     std::vector<VT> ringv(ring + pin, (VT)NAN), x(n, (VT)NAN);
     std::vector<int> chunk_of(n, -1);
+    std::vector<unsigned char> im = img;   // the helpers write the far sums into the images
     int written = 0, kchunk = -1;
     for (const WaveChunk& ch : w.chunks) {
       kchunk++;
@@ -97,20 +104,32 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
       CHECK(ch.img_bytes <= stage_cap || ch.nrows == 1, "stage capacity %d > %d", ch.img_bytes, stage_cap);
       CHECK(ch.nrows >= 1 && ch.nrows <= rows_max, "rows per chunk");
       CHECK(ch.pos0 == written, "chunk positions contiguous");
-      const unsigned char* st = &img[ch.img_off];
-      // the producer warp's gather of the chunk's far values (rows finished in earlier chunks)
-      CHECK(ch.far_off % 16 == 0 && ch.far_off >= ch.img_bytes, "far values after the image");
-      CHECK(ch.nrows == 1 || ch.far_off + (long long)ch.nfar * vtb <= stage_cap, "far values inside the stage");
-      CHECK(ch.far_base >= 0 && ch.far_base + ch.nfar <= (int)w.far_rows.size(), "far list range");
-      std::vector<VT> farv(ch.nfar);
-      for (int f = 0; f < ch.nfar; f++) {
-        const int j = w.far_rows[ch.far_base + f];
-        CHECK(j >= 0 && j < n && !std::isnan((double)x[j]), "far source %d not solved before its chunk", j);
-        // with the library's ring the producer gathers a chunk's far values up to
-        // kWaveMaxStages chunks ahead: their rows must be that much older
-        if (ring == kWaveRing)
-          CHECK(chunk_of[j] <= kchunk - kWaveMaxStages, "far source %d too recent for the gather", j);
-        farv[f] = x[j];
+      unsigned char* st = &im[ch.img_off];
+      if (split) {
+        // a helper block: far sums of the chunk's rows into their right-hand sides, once
+        // the chunks up to far_dep are solved; with the library's ring that is more than
+        // kWaveMaxStages chunks back, so the producer never waits on itself
+        bool any = false;
+        for (int r = 0; r < ch.nrows; r++) {
+          const int p = ch.pos0 + r;
+          VT sum = 0;
+          for (long long e = w.far_ptr[p]; e < w.far_ptr[p + 1]; e++) {
+            const int j = w.far_src[e];
+            CHECK(j >= 0 && j < n && !std::isnan((double)x[j]), "far source %d not solved before its chunk", j);
+            CHECK(chunk_of[j] <= ch.far_dep, "far source %d after the chunk's far_dep", j);
+            sum += (VT)val[w.far_vsrc[e]] * x[j];
+            any = true;
+          }
+          VT br;
+          std::memcpy(&br, st + ch.b_off + (size_t)vtb * r, sizeof(VT));
+          br = lower ? br + sum : br - sum;
+          std::memcpy(st + ch.b_off + (size_t)vtb * r, &br, sizeof(VT));
+        }
+        CHECK(any == (ch.far_dep >= 0), "far_dep marks the chunks with far entries");
+        if (ring - rows_max >= kWaveMaxStages * rows_max)
+          CHECK(ch.far_dep < 0 || ch.far_dep < kchunk - kWaveMaxStages, "far sources too recent for the helpers");
+      } else {
+        CHECK(ch.far_dep < 0, "no far lists without split");
       }
       for (int rr = 0; rr < ch.nrows; rr++) {
         int r = pass == 0 ? rr : ch.nrows - 1 - rr;
@@ -130,8 +149,10 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
           int src;
           std::memcpy(&src, st + meta[2] + (e / lanes) * stride + 4 * lane, 4);
           std::memcpy(&v, st + meta[2] + (e / lanes) * stride + 128 + (size_t)vtb * lane, sizeof(VT));
-          CHECK(src >= 0 && src < ring + pin + ch.nfar, "source slot out of range");
-          VT xv = src < ring + pin ? ringv[src] : farv[src - ring - pin];
+          CHECK(src < ring + pin, "source slot out of range");
+          CHECK(!split || src >= 0, "no global reads in split layouts");
+          VT xv = src >= 0 ? ringv[src] : x[-src - 1];
+          if (src < 0) CHECK(!std::isnan((double)xv), "global source not solved");
           VT prod = v * xv;
           part[g] = (lower || lanes > 1) ? part[g] + prod : part[g] - prod;
         }
@@ -165,9 +186,9 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
       err = std::max(err, (double)std::fabs(x[i] - xr[i]));
       scale = std::max(scale, (double)std::fabs(xr[i]));
     }
-    if (lanes == 1)   // same products in the same order: identical results
+    if (lanes == 1 && !split)   // same products in the same order: identical results
       CHECK(bad == 0, "n=%d band=%d lower=%d pass=%d: %d rows differ", n, band, (int)lower, pass, bad);
-    else              // split sums: a few ulps
+    else                        // split sums: a few ulps
       CHECK(err <= 1e-4 * scale, "n=%d band=%d lower=%d pass=%d lanes=%d err=%g", n, band, (int)lower, pass, lanes,
             err / scale);
   }
@@ -186,9 +207,15 @@ int main() {
         run<double>(n, band, n + band + 2, lower, 64, 16, 4096, 1);
         run<float>(n, band, n + band + 3, lower, 32, 0, 2048, 4);
         run<float>(n, band, n + band + 4, lower, 16, 4096, 2048, 4);
+        // split layouts (far entries summed by helper blocks): the library's ring, and a
+        // ring small enough for far entries on these bands
+        run<float>(n, band, n + band + 7, lower, kWaveRing, kWavePin, st32, 1, true);
+        run<float>(n, band, n + band + 8, lower, 2048, 8, st32, 1, true);
+        run<float>(n, band * 8, n + band + 9, lower, 2048, 64, 8192, 1, true);
       }
     }
   }
+  CHECK(g_far_entries > 0, "the split runs exercise far entries");
   if (fails) {
     fprintf(stderr, "%d failures\n", fails);
     return 1;
