@@ -661,13 +661,16 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     // RG_WAVE_SPLIT=0 keeps them in the images, read from global memory)
     bool split = c->prec == RG_PREC_MIXED && lanes == 1;
     if (const char* e = getenv("RG_WAVE_SPLIT")) split = split && atoi(e) != 0;
+    // pinned slots for far sources (RG_WAVE_PIN lowers the count, for tests and tuning)
+    int pin = kWavePin;
+    if (const char* e = getenv("RG_WAVE_PIN")) pin = std::max(0, std::min(kWavePin, atoi(e)));
     WaveLayout wl, wu;
     std::thread tl([&] {
-      wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, kWavePin, stage_cap, rows_cap,
-                             lanes, split);
+      wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, pin, stage_cap, rows_cap, lanes,
+                             split);
     });
-    wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, kWavePin, stage_cap, rows_cap,
-                           lanes, split);
+    wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, pin, stage_cap, rows_cap, lanes,
+                           split);
     tl.join();
     for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {
       WaveLayout& w = *pr.first;

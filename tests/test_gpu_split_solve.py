@@ -5,7 +5,8 @@ entries are summed by helper blocks into the right-hand side before the
 wavefront block solves the chunk; the result must agree with the oracle's
 PRECO_ILU0::Solve (Preco_ilu0.cpp:497-980) on the same FP32 factors (double
 arithmetic) to FP32 accuracy, and with the unsplit FP32 layout (far sources
-read from global memory by the wavefront block)."""
+read from global memory by the wavefront block).  The pinned-slot table is
+turned off so that this system has far entries at all."""
 
 import ctypes as C
 
@@ -49,6 +50,8 @@ def _factored_context(d):
 
 
 def test_split_fp32_apply_matches_oracle_and_unsplit(monkeypatch):
+    # no pinned slots, so that the far sources of this 200k system are not all pinned
+    monkeypatch.setenv("RG_WAVE_PIN", "0")
     d = _system()
     n = d["num"]["neq"]
     ptr = np.zeros(n + 1, np.int64)
