@@ -657,9 +657,11 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     // rows per chunk: one per consumer thread group (RG_WAVE_ROWS lowers the cap, for tuning)
     int rows_cap = kWaveRows / lanes;
     if (const char* e = getenv("RG_WAVE_ROWS")) rows_cap = std::max(32, std::min(rows_cap, atoi(e)));
-    // FP32 solves of the mixed path: far entries summed by helper blocks (split layouts;
-    // RG_WAVE_SPLIT=0 keeps them in the images, read from global memory)
-    bool split = c->prec == RG_PREC_MIXED && lanes == 1;
+    // solves whose summation order is free (the mixed path's FP32 solves, the FP64 path):
+    // far entries summed by helper blocks (split layouts; RG_WAVE_SPLIT=0 keeps them in
+    // the images, read from global memory).  The reference-storage mode keeps the
+    // reference's order in every row, so its far entries stay in the images.
+    bool split = (c->prec == RG_PREC_MIXED || c->prec == RG_PREC_FP64) && lanes == 1;
     if (const char* e = getenv("RG_WAVE_SPLIT")) split = split && atoi(e) != 0;
     // pinned slots for far sources (RG_WAVE_PIN lowers the count, for tests and tuning)
     int pin = kWavePin;
@@ -689,7 +691,7 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
         TRY(upload(c, d.far_ptr, w.far_ptr.data(), w.far_ptr.size()));
         TRY(upload(c, d.far_src, w.far_src.data(), std::max<size_t>(w.far_src.size(), 1)));
         TRY(upload(c, d.far_vsrc, w.far_vsrc.data(), std::max<size_t>(w.far_vsrc.size(), 1)));
-        TRY(d.far_val.alloc(std::max<size_t>(w.far_src.size(), 1) * sizeof(float)));
+        TRY(d.far_val.alloc(std::max<size_t>(w.far_src.size(), 1) * (size_t)vtb));
         TRY(d.chunk_ready.alloc(std::max<size_t>(w.chunks.size(), 1)));
         TRY(cudaMemsetAsync(d.chunk_ready.p, 0, d.chunk_ready.bytes(), c->st));
         TRY(d.progress.alloc(1));

@@ -17,7 +17,7 @@
 // Levels too large for a stage are split into consecutive chunks (rows of one
 // level do not depend on each other).
 //
-// FP32 solves (whose summation order is free) use split layouts: entries whose
+// Solves whose summation order is free (FP32 and FP64) use split layouts: entries whose
 // source lies outside the ring and the pinned slots -- about a fifth of them
 // on the 4M-triangle river -- are not in the images.  The same cooperative
 // launch then holds helper blocks: a helper takes a future chunk once the
@@ -496,7 +496,7 @@ static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, con
   const int nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
   const size_t smem = (kWaveRing + kWavePin) * sizeof(VT) + (size_t)nst * (size_t)wd.stage_bytes;
   if (wd.split) {
-    if (sizeof(VT) != 4 || wd.lanes != 1) return cudaErrorInvalidValue;   // split layouts: FP32, one lane per row
+    if (wd.lanes != 1) return cudaErrorInvalidValue;   // split layouts: one lane per row
     return launch_wave_k<VT, LOWER, 1, false, true>(c, wd, x, ks, smem);
   }
   const bool far = wd.ring_misses > 0;
@@ -534,8 +534,12 @@ cudaError_t launch_wave_pack(rg_ctx* c) {
   for (WaveDev* wd : {&c->waveL, &c->waveU}) {
     if (wd->split && wd->nfar > 0) {
       const int nbf = (int)std::min<long long>((wd->nfar + 255) / 256, (long long)c->num_sms * 8);
-      k_pack_far<float, float><<<nbf, 256, 0, rg_counted(c)>>>(wd->nfar, wd->far_vsrc.p, c->LU32.p,
-                                                                 reinterpret_cast<float*>(wd->far_val.p));
+      if (c->prec == RG_PREC_FP64)
+        k_pack_far<double, double><<<nbf, 256, 0, rg_counted(c)>>>(wd->nfar, wd->far_vsrc.p, c->LU64.p,
+                                                                     reinterpret_cast<double*>(wd->far_val.p));
+      else
+        k_pack_far<float, float><<<nbf, 256, 0, rg_counted(c)>>>(wd->nfar, wd->far_vsrc.p, c->LU32.p,
+                                                                   reinterpret_cast<float*>(wd->far_val.p));
     }
     int nb = (int)std::min<long long>((wd->nent + 255) / 256 + 1, (long long)c->num_sms * 8);
     if (c->prec == RG_PREC_FP64)

@@ -212,6 +212,7 @@ int main() {
         run<float>(n, band, n + band + 7, lower, kWaveRing, kWavePin, st32, 1, true);
         run<float>(n, band, n + band + 8, lower, 2048, 8, st32, 1, true);
         run<float>(n, band * 8, n + band + 9, lower, 2048, 64, 8192, 1, true);
+        run<double>(n, band * 8, n + band + 10, lower, 2048, 64, st64, 1, true);
       }
     }
   }

@@ -77,7 +77,8 @@ def test_device_wait_limit_runs_out_and_context_recovers(monkeypatch):
     assert "waited for" in str(ei.value)
     ctx.set_wait_limit(0)
     x = ctx.ilu0_apply(b)
-    assert np.array_equal(x, ref)
+    # the dependency-driven solves sum in their own order: equal to rounding
+    assert np.max(np.abs(x - ref)) <= 1e-12 * np.max(np.abs(ref))
     ctx.close()
 
 

@@ -31,10 +31,10 @@ def _system():
     return out
 
 
-def _factored_context(d):
+def _factored_context(d, precision=_lib.PREC_MIXED):
     m, num, mod, bnd, st = d["mesh"], d["num"], d["mod"], d["bnd"], d["st"]
     ctx = _lib.Context(m.x, m.y, mod["elem_nodes"], mod["elem_nnd"], mod["elem_flag"], mod["elem_vt"], 9.81, 0.005,
-                       Params().vk, precision=_lib.PREC_MIXED)
+                       Params().vk, precision=precision)
     ctx.set_pattern(num["width"], num["index"], num["eqno"])
     ctx.set_boundary(bnd["nflag"], bnd["bckind"], bnd["rot4"], mod["niox"], mod["nioy"], bnd["bcU"], bnd["bcS"])
     z0 = np.zeros(m.np)
@@ -73,3 +73,23 @@ def test_split_fp32_apply_matches_oracle_and_unsplit(monkeypatch):
         assert np.max(np.abs(x - x0)) <= 1e-4 * scale
     ctx.close()
     ctx0.close()
+
+
+def test_split_fp64_apply_matches_oracle(monkeypatch):
+    """The FP64 path splits too (its summation order is free; only the reference-
+    storage mode keeps the reference's order): equal to the oracle's FP64 solve to
+    rounding."""
+    monkeypatch.setenv("RG_WAVE_PIN", "0")
+    d = _system()
+    n = d["num"]["neq"]
+    ptr = np.zeros(n + 1, np.int64)
+    ptr[1:] = np.cumsum(d["num"]["width"])
+    ctx, LU, stats = _factored_context(d, _lib.PREC_FP64)
+    assert stats[8] > 0 and stats[9] > 0
+    rng = np.random.default_rng(6)
+    for _ in range(2):
+        b = rng.standard_normal(n)
+        x = ctx.ilu0_apply(b)
+        ref = oracle.ilu0_solve(ptr, d["num"]["index"], LU, b)
+        assert np.max(np.abs(x - ref)) <= 1e-11 * np.max(np.abs(ref))
+    ctx.close()
