@@ -647,8 +647,8 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
   {
     const int vtb = (c->prec == RG_PREC_MIXED) ? 4 : 8;
     // stages: what the shared-memory budget leaves after the ring and pinned slots
-    const int nst = (vtb == 8) ? kWaveStages64 : kWaveStages32;
-    const int stage_cap = (int)(((kWaveSmem - (long long)(kWaveRing + kWavePin) * vtb) / nst) & ~255ll);
+    const int nst = wave_stages(vtb), ring = wave_ring(vtb);
+    const int stage_cap = (int)(((kWaveSmem - (long long)(ring + wave_pin(vtb)) * vtb) / nst) & ~255ll);
     std::vector<int> diag_pos(rowptr.begin(), rowptr.end() - 1);
     // threads per row (RG_WAVE_LANES = 1, 2 or 4 overrides it for the FP32 solve, for tuning)
     int lanes = (vtb == 8) ? kWaveLanes64 : kWaveLanes32;
@@ -664,14 +664,14 @@ static rg_status set_pattern_impl(rg_ctx* c, int neq, const int* width, const in
     bool split = (c->prec == RG_PREC_MIXED || c->prec == RG_PREC_FP64) && lanes == 1;
     if (const char* e = getenv("RG_WAVE_SPLIT")) split = split && atoi(e) != 0;
     // pinned slots for far sources (RG_WAVE_PIN lowers the count, for tests and tuning)
-    int pin = kWavePin;
-    if (const char* e = getenv("RG_WAVE_PIN")) pin = std::max(0, std::min(kWavePin, atoi(e)));
+    int pin = wave_pin(vtb);
+    if (const char* e = getenv("RG_WAVE_PIN")) pin = std::max(0, std::min(wave_pin(vtb), atoi(e)));
     WaveLayout wl, wu;
     std::thread tl([&] {
-      wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, kWaveRing, pin, stage_cap, rows_cap, lanes,
+      wl = build_wave_layout(neq, Lptr, Lcol, Lsrc, diag_pos, true, vtb, ring, pin, stage_cap, rows_cap, lanes,
                              split);
     });
-    wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, kWaveRing, pin, stage_cap, rows_cap, lanes,
+    wu = build_wave_layout(neq, Uptr, Ucol, Usrc, diag_pos, false, vtb, ring, pin, stage_cap, rows_cap, lanes,
                            split);
     tl.join();
     for (auto pr : {std::make_pair(&wl, &c->waveL), std::make_pair(&wu, &c->waveU)}) {

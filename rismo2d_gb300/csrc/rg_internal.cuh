@@ -74,11 +74,15 @@ constexpr int kWaveSlice = 32;      // rows per warp slice
 constexpr int kWaveThreads = 544;   // one CTA: 16 consumer warps + 1 producer warp
 constexpr int kWaveRows = kWaveThreads - 32;   // rows per chunk at most (one per consumer thread)
 constexpr int kWaveMaxStages = 8;
-// shared-memory stages in flight: the double ring leaves room for two large ones
-constexpr int kWaveStages32 = 3, kWaveStages64 = 2;
-// shared-memory ring of solved values and pinned slots for far sources
-constexpr int kWaveRing = 16384;
-constexpr int kWavePin = 4096;
+// shared-memory ring of solved values and pinned slots for far sources, per value
+// size: the FP64 ring holds half the slots so that both solves keep three stages
+// in flight (the solve's rate is bounded by the copies in flight)
+constexpr int kWaveRing = 16384, kWaveRing64 = 8192;
+constexpr int kWavePin = 4096, kWavePin64 = 2048;
+constexpr int kWaveStages32 = 3, kWaveStages64 = 3;
+constexpr int wave_ring(int vtb) { return vtb == 8 ? kWaveRing64 : kWaveRing; }
+constexpr int wave_pin(int vtb) { return vtb == 8 ? kWavePin64 : kWavePin; }
+constexpr int wave_stages(int vtb) { return vtb == 8 ? kWaveStages64 : kWaveStages32; }
 // dynamic shared memory available to the wavefront kernel
 constexpr int kWaveSmem = 232448 - 2048;
 struct WaveLayout {

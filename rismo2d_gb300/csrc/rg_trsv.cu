@@ -31,6 +31,7 @@
 #include "rg_internal.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 namespace {
@@ -41,9 +42,16 @@ constexpr int kThreads = kWaveThreads;
 // has finished them before its producer stages the chunk, so a helper can always
 // complete a chunk the producer waits for
 static_assert(kWaveRing - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helper blocks");
+static_assert(kWaveRing64 - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helper blocks");
+static_assert(kWaveStages32 <= kWaveMaxStages && kWaveStages64 <= kWaveMaxStages, "stage table");
 constexpr long long kMbarSpin = 1ll << 26;
 constexpr long long kFlagSpin = 1ll << 24;   // polls of a global flag (~10 s at L2 latency)
 constexpr long long kDrainSpin = 1ll << 16;
+// launch options of the wavefront solve, packed in one int: bits 0-7 the chunk
+// images prefetched into L2 ahead of the stages, bit 8 progress published by a
+// thread of the producer warp (split layouts), bits 16-30 the helper blocks'
+// back-off in ns between polls of a progress word still more than 4 chunks short
+constexpr int kWavePrefetch = 8, kWavePublish = 1, kWaveBackoffNs = 0;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -79,6 +87,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
           smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
       : "memory");
+}
+
+// global -> L2 prefetch of a chunk image (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, int bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ uint64_t policy_evict_first() {
@@ -177,6 +190,14 @@ __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned l
 __device__ __forceinline__ void st_release_s32(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ void st_release_cta_shared(int* p, int v) {
+  asm volatile("st.release.cta.shared::cta.s32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_cta_shared(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.s32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
+  return v;
+}
 // generic-proxy writes to global memory before async-proxy (TMA) reads of it
 __device__ __forceinline__ void fence_proxy_async_global() {
   asm volatile("fence.proxy.async.global;" ::: "memory");
@@ -191,7 +212,7 @@ __device__ void wave_helper(int nchunks, const WaveChunk* __restrict__ chunks, u
                             const VT* __restrict__ x, int* err, const long long* __restrict__ far_ptr,
                             const int* __restrict__ far_src, const VT* __restrict__ far_val,
                             const int* __restrict__ bidx, int* chunk_ready, const unsigned long long* progress,
-                            unsigned epoch) {
+                            unsigned epoch, int backoff_ns) {
   __shared__ int s_go;
   const int H = gridDim.x - 1;
   VT* bimg = reinterpret_cast<VT*>(img);
@@ -202,7 +223,9 @@ __device__ void wave_helper(int nchunks, const WaveChunk* __restrict__ chunks, u
       const unsigned long long need = ((unsigned long long)epoch << 32) | (unsigned long long)(ch.far_dep + 1);
       long long it = 0;
       int go = 1;
-      while (ld_acquire_u64(progress) < need) {
+      unsigned long long cur;
+      while ((cur = ld_acquire_u64(progress)) < need) {
+        if (backoff_ns > 0 && need - cur > 4) __nanosleep((unsigned)backoff_ns);
         if ((++it & 1023) == 0 && *reinterpret_cast<volatile int*>(err) != 0) {
           go = 0;
           break;
@@ -240,15 +263,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_trsv_wave(int nchunks, const WaveChunk* __restrict__ chunks, unsigned char* img, VT* __restrict__ x,
                 int stage_bytes, int* err, const KrylovScalars* ks, const long long* __restrict__ far_ptr,
                 const int* __restrict__ far_src, const VT* __restrict__ far_val, const int* __restrict__ bidx,
-                int* chunk_ready, unsigned long long* progress, unsigned epoch) {
+                int* chunk_ready, unsigned long long* progress, unsigned epoch, int tune) {
   if (ks && ks->conv != 0) return;
   if (SPLIT && blockIdx.x > 0) {
     wave_helper<VT, LOWER>(nchunks, chunks, img, x, err, far_ptr, far_src, far_val, bidx, chunk_ready, progress,
-                           epoch);
+                           epoch, tune >> 16);
     return;
   }
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr int RING = kWaveRing, PIN = kWavePin, nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
+  constexpr int RING = wave_ring(sizeof(VT)), PIN = wave_pin(sizeof(VT)), nst = wave_stages(sizeof(VT));
   constexpr int kConsumers = kThreads - 32;
   constexpr int kStride = kWaveSlice * (4 + (int)sizeof(VT));   // bytes per entry column of a slice
   static_assert((RING & (RING - 1)) == 0, "ring size must be a power of two");
@@ -261,7 +284,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ WaveChunk sdesc[kWaveMaxStages];
   __shared__ int s_issued;   // copies the producer has started
   __shared__ int s_abort;    // set by a consumer whose wait ran out (read after a barrier)
+  __shared__ int s_done;     // chunks the consumers have completed (publisher mode)
   const int tid = threadIdx.x;
+  const int prefetch = tune & 255;
+  const bool publish = SPLIT && ((tune >> 8) & 1) != 0;
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
@@ -269,6 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     s_issued = 0;
     s_abort = 0;
+    s_done = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -280,10 +307,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (tid == kConsumers && nchunks > 0) {
       const uint64_t pol = policy_evict_first();
       WaveChunk next = chunks[0];
+      // the images of the first chunks into L2 ahead of their stages
+      for (int q = 1; q < prefetch && q < nchunks; q++) bulk_prefetch_l2(img + chunks[q].img_off, chunks[q].img_bytes);
       for (int k = 0; k < nchunks; k++) {
         const int s = k % nst;
         const WaveChunk ch = next;
         if (k + 1 < nchunks) next = chunks[k + 1];   // descriptor load overlaps the wait below
+        if (prefetch > 0 && k + prefetch < nchunks) {
+          const WaveChunk ahead = chunks[k + prefetch];
+          bulk_prefetch_l2(img + ahead.img_off, ahead.img_bytes);
+        }
         if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
           wave_wait_failed(err, LOWER ? 30 : 31, k);
           *v_abort = 1;
@@ -316,6 +349,24 @@ __global__ void __launch_bounds__(kThreads, 1)
         fence_proxy_async();   // earlier generic reads of the stage precede the async refill
         mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
         bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
+      }
+    } else if (publish && tid == kConsumers + 1) {
+      // ---- publisher: the consumers' chunk count to the helper blocks -----------
+      // The consumers' x stores precede their barrier and thread 0's CTA-scope
+      // release of s_done; this thread's acquire of it and its GPU-scope release of
+      // the progress word carry them to the helpers (the fence stays off the
+      // consumers' path).  Bounded: ends at the last chunk, on an abort or an error.
+      int seen = 0;
+      long long it = 0;
+      while (seen < nchunks) {
+        const int d = ld_acquire_cta_shared(&s_done);
+        if (d > seen) {
+          seen = d;
+          st_release_u64(progress, ((unsigned long long)epoch << 32) | (unsigned long long)d);
+          it = 0;
+        } else if ((++it & 1023) == 0 && (*v_abort || *reinterpret_cast<volatile int*>(err) != 0 || it > kMbarSpin)) {
+          break;
+        }
       }
     }
     return;
@@ -400,8 +451,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     consumers_sync();                 // chunk k complete: its values are visible, its stage is free
     // publish the progress for the helper blocks (x stores of the chunk precede it)
     if (SPLIT && tid == 0) {
-      __threadfence();
-      st_release_u64(progress, ((unsigned long long)epoch << 32) | (unsigned long long)(k + 1));
+      if (publish) {
+        st_release_cta_shared(&s_done, k + 1);
+      } else {
+        __threadfence();
+        st_release_u64(progress, ((unsigned long long)epoch << 32) | (unsigned long long)(k + 1));
+      }
     }
     if (*v_abort) {
       // a copy never completed: stop, after giving the copies already started a bounded time to land
@@ -467,9 +522,21 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
   int* ready = wd.chunk_ready.p;
   unsigned long long* prog = wd.progress.p;
   unsigned epoch = 0;
+  // launch options (tuning overrides: RG_WAVE_PREFETCH chunks, 0 = none;
+  // RG_WAVE_PUBLISH 0/1; RG_WAVE_BACKOFF ns)
+  static int tune = -1;
+  if (tune < 0) {
+    const char* e = getenv("RG_WAVE_PREFETCH");
+    const int pf = e ? std::max(0, std::min(64, atoi(e))) : kWavePrefetch;
+    e = getenv("RG_WAVE_PUBLISH");
+    const int pub = e ? (atoi(e) != 0) : kWavePublish;
+    e = getenv("RG_WAVE_BACKOFF");
+    const int bo = e ? std::max(0, std::min(20000, atoi(e))) : kWaveBackoffNs;
+    tune = pf | (pub << 8) | (bo << 16);
+  }
   if (!SPLIT) {
     kern<<<1, kThreads, smem, rg_counted(c)>>>(nchunks, chunks, img, x, stage_bytes, err, ks, fptr, fsrc, fval, bidx,
-                                               ready, prog, epoch);
+                                               ready, prog, epoch, tune);
     return cudaGetLastError();
   }
   // one wavefront block and a helper block on every other SM, all co-resident
@@ -483,7 +550,7 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
   int blocks = std::max(2, std::min(blocks_dev[c->device], c->num_sms));
   epoch = ++wd.epoch;
   void* args[] = {&nchunks, &chunks, &img, &x, &stage_bytes, &err, &ks, &fptr, &fsrc, &fval, &bidx, &ready, &prog,
-                  &epoch};
+                  &epoch, &tune};
   return cudaLaunchCooperativeKernel((void*)kern, blocks, kThreads, args, smem, rg_counted(c));
 }
 
@@ -493,8 +560,8 @@ static cudaError_t launch_wave_t(rg_ctx* c, WaveDev& wd, const VT* b, VT* x, con
   int nb = (n + 255) / 256;
   if (nb > c->num_sms * 4) nb = c->num_sms * 4;
   k_gather_lev<VT><<<nb, 256, 0, rg_counted(c)>>>(n, wd.order.p, wd.bidx.p, b, reinterpret_cast<VT*>(wd.img.p), ks);
-  const int nst = sizeof(VT) == 8 ? kWaveStages64 : kWaveStages32;
-  const size_t smem = (kWaveRing + kWavePin) * sizeof(VT) + (size_t)nst * (size_t)wd.stage_bytes;
+  const int nst = wave_stages(sizeof(VT));
+  const size_t smem = (size_t)(wave_ring(sizeof(VT)) + wave_pin(sizeof(VT))) * sizeof(VT) + (size_t)nst * (size_t)wd.stage_bytes;
   if (wd.split) {
     if (wd.lanes != 1) return cudaErrorInvalidValue;   // split layouts: one lane per row
     return launch_wave_k<VT, LOWER, 1, false, true>(c, wd, x, ks, smem);

@@ -195,14 +195,16 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
 }
 
 int main() {
-  const int st32 = 49408, st64 = 33280;   // the stage sizes of the library's shared-memory budget
+  // the stage sizes of the library's shared-memory budget
+  const int st32 = (int)(((kWaveSmem - (long long)(kWaveRing + kWavePin) * 4) / kWaveStages32) & ~255ll);
+  const int st64 = (int)(((kWaveSmem - (long long)(kWaveRing64 + kWavePin64) * 8) / kWaveStages64) & ~255ll);
   for (int lower = 0; lower < 2; lower++) {
     for (int n : {1, 2, 7, 64, 1000, 20000}) {
       for (int band : {1, 3, 50, 600}) {
-        run<double>(n, band, n + band, lower, kWaveRing, kWavePin, st64, kWaveLanes64);
+        run<double>(n, band, n + band, lower, kWaveRing64, kWavePin64, st64, kWaveLanes64);
         run<float>(n, band, n + band + 1, lower, kWaveRing, kWavePin, st32, kWaveLanes32);
         run<float>(n, band, n + band + 5, lower, kWaveRing, kWavePin, st32, 1);
-        run<double>(n, band, n + band + 6, lower, kWaveRing, kWavePin, st64, 2);
+        run<double>(n, band, n + band + 6, lower, kWaveRing64, kWavePin64, st64, 2);
         // tiny rings, pinned tables and stages force pinning, global reads and level splitting
         run<double>(n, band, n + band + 2, lower, 64, 16, 4096, 1);
         run<float>(n, band, n + band + 3, lower, 32, 0, 2048, 4);
@@ -210,6 +212,7 @@ int main() {
         // split layouts (far entries summed by helper blocks): the library's ring, and a
         // ring small enough for far entries on these bands
         run<float>(n, band, n + band + 7, lower, kWaveRing, kWavePin, st32, 1, true);
+        run<double>(n, band, n + band + 11, lower, kWaveRing64, kWavePin64, st64, 1, true);
         run<float>(n, band, n + band + 8, lower, 2048, 8, st32, 1, true);
         run<float>(n, band * 8, n + band + 9, lower, 2048, 64, 8192, 1, true);
         run<double>(n, band * 8, n + band + 10, lower, 2048, 64, st64, 1, true);
