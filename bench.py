@@ -375,6 +375,168 @@ def trsv_roofline(prof, neq, nnz, tri, nodes, dev_ms_total):
 
 # ---- main ---------------------------------------------------------------------------
 
+def _step_timed(sim, t, dt, kw):
+    import torch
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    rep = sim.step(t, dt, **kw)
+    return rep, time.perf_counter() - a
+
+
+def _state_errs(sa, sb, z):
+    """Max errors of state `sa` against `sb`: U and V relative to the field's maximum
+    magnitude, depth H = S - z relative to the maximum depth (over nodes wet in both),
+    and the number of nodes whose dry flag differs."""
+    wa, wb = (sa["flag"] & 64) == 0, (sb["flag"] & 64) == 0
+    w = wa & wb
+    out = {}
+    for v in ("U", "V"):
+        den = max(float(np.max(np.abs(sb[v][w]))), 1e-30)
+        out[v] = float(np.max(np.abs(sa[v][w] - sb[v][w]))) / den
+    hb = sb["S"][w] - z[w]
+    out["H"] = float(np.max(np.abs(sa["S"][w] - sb["S"][w]))) / max(float(np.max(hb)), 1e-30)
+    out["dry_flags_differing"] = int(np.count_nonzero(wa != wb))
+    return out
+
+
+def study_precision(nsteps: int, ref_steps: int) -> dict:
+    """The precision configuration: the meander refined to 1,002,174 triangles, unsteady
+    (dt = 10 s, Q(t) = 300 + 500 sin^2(pi t / 7200)), `nsteps` time steps of the mixed path
+    and of the FP64 path run side by side from the same initial state, both with the
+    headline's Newton-Krylov options and Newton to ||B||/||B_0|| <= 1e-8; per step the
+    mixed state's error against the FP64 state.  The first `ref_steps` steps are also run
+    with the plain FP64 reference algorithm (exact linear solves, factor every iteration,
+    the reference's Jacobian) to show that the options leave the converged state alone."""
+    from rismo2d_gb300 import _lib, meshgen
+    from rismo2d_gb300.sim import Params, Simulation, RG_CRIT_RESIDUAL
+    mesh = meshgen.meander(nx=2831, ny=177)
+    hyd = meshgen.sin2_hydrograph()
+    dt = 10.0
+    opts = dict(criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL, linear_forcing=LINEAR_FORCING,
+                ilu_reuse=ILU_REUSE, friction_jacobian=True)
+    ref = dict(criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL)
+    sims = {"mixed": Simulation(mesh, Params(), hydrograph=hyd, precision=_lib.PREC_MIXED),
+            "fp64": Simulation(mesh, Params(), hydrograph=hyd, precision=_lib.PREC_FP64)}
+    if ref_steps > 0:
+        sims["fp64_reference_algorithm"] = Simulation(mesh, Params(), hydrograph=hyd, precision=_lib.PREC_FP64)
+    for sim in sims.values():
+        sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+    rows, t = [], 0.0
+    for k in range(nsteps):
+        row = {"step": k}
+        st = {}
+        for name, sim in sims.items():
+            if name == "fp64_reference_algorithm" and k >= ref_steps:
+                continue
+            rep, secs = _step_timed(sim, t, dt, ref if name == "fp64_reference_algorithm" else opts)
+            st[name] = sim.get_state()
+            row[name] = {"s": round(secs, 3), "newton": rep["newton_iterations"], "krylov": rep["krylov_iterations"],
+                         "converged": bool(rep["converged"])}
+        row["mixed_vs_fp64"] = _state_errs(st["mixed"], st["fp64"], mesh.z)
+        if "fp64_reference_algorithm" in st:
+            row["fp64_vs_fp64_reference_algorithm"] = _state_errs(st["fp64"], st["fp64_reference_algorithm"], mesh.z)
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+        t += dt
+    for sim in sims.values():
+        sim.close()
+    worst = {v: max(r["mixed_vs_fp64"][v] for r in rows) for v in ("U", "V", "H")}
+    worst["dry_flags_differing"] = max(r["mixed_vs_fp64"]["dry_flags_differing"] for r in rows)
+    mean = lambda arm, key: round(float(np.mean([r[arm][key] for r in rows if arm in r])), 3)
+    return {"study": "precision1m", "mesh": {"triangles": int(mesh.ne), "nodes": int(mesh.np)},
+            "steps": nsteps, "dt": dt, "worst_mixed_vs_fp64": worst,
+            "per_step_mean": {arm: {"s": mean(arm, "s"), "newton": mean(arm, "newton"), "krylov": mean(arm, "krylov")}
+                              for arm in sims},
+            "all_converged": all(r[a]["converged"] for r in rows for a in sims if a in r),
+            "rows": rows}
+
+
+def study_learned(train_steps: int, test_steps: int, every: int) -> dict:
+    """The learned configuration: the meander at 1,002,174 triangles with seeded random
+    bump fields.  Training: 4 flood waves (peaks U(400, 1200) m^3/s, seeds 10-13, each on
+    its own bump field of the same seed), `train_steps` steps each of the mixed solver with
+    the headline options from rest; every `every`-th time-level triple becomes training
+    samples.  Held out: 2 flood waves (seeds 20, 21) on their own bump fields, run cold and
+    with the learned warm start for `test_steps` steps; Newton, Krylov and seconds per step
+    and the final states' difference."""
+    from rismo2d_gb300 import _lib, meshgen
+    from rismo2d_gb300 import warmstart as ws
+    from rismo2d_gb300.sim import Params, Simulation, RG_CRIT_RESIDUAL
+    dt, period = 10.0, 2000.0
+    opts = dict(criterion=RG_CRIT_RESIDUAL, residual_tol=RESIDUAL_TOL, linear_forcing=LINEAR_FORCING,
+                ilu_reuse=ILU_REUSE, friction_jacobian=True)
+
+    def case(seed):
+        mesh = meshgen.meander(nx=2831, ny=177, bumps=400, bump_seed=seed, bump_amp=(0.05, 0.25))
+        peak = float(np.random.default_rng(seed).uniform(400.0, 1200.0))
+        hyd = meshgen.sin2_hydrograph(Q0=300.0, dQ=peak - 300.0, period=period, t_end=period, every=100.0)
+        return mesh, hyd, peak
+
+    net = None
+    info = {"train": [], "held_out": []}
+    t0 = time.perf_counter()
+    nsamp = 0
+    for seed in (10, 11, 12, 13):
+        mesh, hyd, peak = case(seed)
+        sim = Simulation(mesh, Params(), hydrograph=hyd, precision=_lib.PREC_MIXED)
+        sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+        states, times, reps = ws.collect_trajectory(sim, hyd, 0.0, dt, train_steps, **opts)
+        sim.close()
+        if net is None:
+            net = ws.WarmStartNet(mesh, seed=7)
+            net.set_scales((4.0, 1.0, 1.0), *ws.trajectory_scales(states))
+        else:
+            net.set_bed(mesh)
+        for k in range(2, len(states), every):
+            qn, qp = ws.discharge_ratios(hyd, times[k - 1], dt)
+            nsamp += net.add_triple(states[k - 2], states[k - 1], states[k], qn, qp)
+        info["train"].append({"seed": seed, "peak": round(peak, 1), "steps": train_steps,
+                              "newton_per_step": round(float(np.mean([r["newton_iterations"] for r in reps])), 2),
+                              "converged": all(r["converged"] for r in reps)})
+        print(json.dumps(info["train"][-1]), file=sys.stderr, flush=True)
+    t1 = time.perf_counter()
+    losses = net.train(epochs=TRAIN_EPOCHS, batch=TRAIN_BATCH, lr=1e-3, seed=3)
+    t2 = time.perf_counter()
+    info.update(samples=int(nsamp), epochs=TRAIN_EPOCHS, loss_first_last=[round(float(losses[0]), 4),
+                                                                          round(float(losses[-1]), 4)],
+                trajectory_s=round(t1 - t0, 1), train_s=round(t2 - t1, 1))
+    for seed in (20, 21):
+        mesh, hyd, peak = case(seed)
+        net.set_bed(mesh)
+        res = {"seed": seed, "peak": round(peak, 1), "steps": test_steps}
+        finals = {}
+        for arm in ("cold", "learned"):
+            sim = Simulation(mesh, Params(), hydrograph=hyd, precision=_lib.PREC_MIXED)
+            sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+            hist = [sim.get_state()]
+            newton, krylov, secs, conv, t = [], [], [], [], 0.0
+            for k in range(test_steps):
+                a = time.perf_counter()
+                if arm == "learned" and len(hist) >= 2:
+                    sim.set_warm_start(*ws.predict_next(net, hist[-2], hist[-1], t, hyd, dt))
+                rep = sim.step(t, dt, **opts)
+                st = sim.get_state()
+                secs.append(time.perf_counter() - a)
+                hist = [hist[-1], st]
+                newton.append(rep["newton_iterations"])
+                krylov.append(rep["krylov_iterations"])
+                conv.append(bool(rep["converged"]))
+                t += dt
+            finals[arm] = hist[-1]
+            sim.close()
+            sl = slice(2, None)   # the first two steps have no prediction
+            res[arm] = {"newton_per_step": round(float(np.mean(newton[sl])), 2),
+                        "krylov_per_step": round(float(np.mean(krylov[sl])), 2),
+                        "s_per_step": round(float(np.mean(secs[sl])), 3), "converged": all(conv)}
+        res["learned_speedup"] = round(res["cold"]["s_per_step"] / res["learned"]["s_per_step"], 3)
+        res["learned_vs_cold_final"] = _state_errs(finals["learned"], finals["cold"], mesh.z)
+        info["held_out"].append(res)
+        print(json.dumps(res), file=sys.stderr, flush=True)
+    net.close()
+    return {"study": "learned1m", "dt": dt, "hydrograph": f"Q(t) = 300 + (peak - 300) sin^2(pi t / {period:.0f})",
+            "bed": "meander + 400 Gaussian bumps (0.05-0.25 m, sigma 30 m) per seed", **info}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -390,8 +552,21 @@ def main():
     ap.add_argument("--linear-forcing", type=float, default=LINEAR_FORCING)
     ap.add_argument("--ilu-reuse", type=int, default=ILU_REUSE)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU solver sampling (0: skip)")
+    ap.add_argument("--study", choices=("precision1m", "learned1m"), default=None,
+                    help="run a study at 1M triangles instead of the benchmark (one JSON line)")
+    ap.add_argument("--study-steps", type=int, default=50)
+    ap.add_argument("--study-ref-steps", type=int, default=2)
+    ap.add_argument("--study-train-steps", type=int, default=100)
+    ap.add_argument("--study-test-steps", type=int, default=30)
+    ap.add_argument("--study-every", type=int, default=2)
     args = ap.parse_args()
     warmup = max(3, args.warmup)
+    if args.study == "precision1m":
+        print(json.dumps(study_precision(args.study_steps, args.study_ref_steps)), flush=True)
+        return 0
+    if args.study == "learned1m":
+        print(json.dumps(study_learned(args.study_train_steps, args.study_test_steps, args.study_every)), flush=True)
+        return 0
     wl = workloads()[args.workload]
 
     if args.impl == "reference":

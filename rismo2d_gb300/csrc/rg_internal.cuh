@@ -71,8 +71,9 @@ struct WaveChunk {
   int pad0, pad1, pad2, pad3;
 };
 constexpr int kWaveSlice = 32;      // rows per warp slice
-constexpr int kWaveThreads = 544;   // one CTA: 16 consumer warps + 1 producer warp
-constexpr int kWaveRows = kWaveThreads - 32;   // rows per chunk at most (one per consumer thread)
+// one CTA: 16 consumer warps, a producer warp and a publisher warp
+constexpr int kWaveRows = 512;      // rows per chunk at most (one per consumer thread)
+constexpr int kWaveThreads = kWaveRows + 64;
 constexpr int kWaveMaxStages = 8;
 // shared-memory ring of solved values and pinned slots for far sources, per value
 // size: the FP64 ring holds half the slots so that both solves keep three stages

@@ -37,6 +37,7 @@
 namespace {
 
 constexpr int kThreads = kWaveThreads;
+constexpr int kConsumers = kWaveRows;   // warps 0-15; warp 16 produces, warp 17 publishes
 // a chunk's far sources lie at least the ring's reach (kWaveRing - kWaveRows
 // positions, so more than kWaveMaxStages chunks) before it: the wavefront block
 // has finished them before its producer stages the chunk, so a helper can always
@@ -48,10 +49,13 @@ constexpr long long kMbarSpin = 1ll << 26;
 constexpr long long kFlagSpin = 1ll << 24;   // polls of a global flag (~10 s at L2 latency)
 constexpr long long kDrainSpin = 1ll << 16;
 // launch options of the wavefront solve, packed in one int: bits 0-7 the chunk
-// images prefetched into L2 ahead of the stages, bit 8 progress published by a
-// thread of the producer warp (split layouts), bits 16-30 the helper blocks'
-// back-off in ns between polls of a progress word still more than 4 chunks short
-constexpr int kWavePrefetch = 8, kWavePublish = 1, kWaveBackoffNs = 0;
+// images prefetched into L2 ahead of the stages, bit 8 progress published by the
+// publisher warp (split layouts), bits 9-13 the chunk flags the producer reads
+// ahead in one batch (split layouts; 0 = one acquire per chunk), bits 16-30 the
+// helper blocks' back-off in ns between polls of a progress word still more than
+// 4 chunks short
+constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWaveBackoffNs = 0;
+static_assert(kWaveScan < 32, "scan width field");
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -140,13 +144,15 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, unsigned pari
 }
 
 __device__ __forceinline__ void consumers_sync() {
-  asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");
+  asm volatile("bar.sync 1, %0;" ::"r"(kConsumers) : "memory");
 }
 
-// Warp-specialised wavefront solve: warp 31 (one elected lane) is the producer
+// Warp-specialised wavefront solve: warp 16 (one elected lane) is the producer
 // that streams chunk images into NST shared-memory stages with cp.async.bulk;
-// warps 0..30 consume the stages in order, one dependency-level chunk at a
-// time, one row per thread, synchronising on a named barrier between chunks.
+// warps 0..15 consume the stages in order, one dependency-level chunk at a
+// time, one row per thread, synchronising on a named barrier between chunks;
+// with split layouts one lane of warp 17 publishes the consumers' progress to
+// the helper blocks.
 //
 // Row r of a chunk is solved by consumer thread r: its entries sit in its warp
 // slice column by column, so the 32 lanes of a warp read consecutive words.
@@ -179,6 +185,13 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ int ld_relaxed_s32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// with the relaxed loads before it, an acquire of what they observed
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ int ld_acquire_s32(const int* p) {
   int v;
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -218,7 +231,10 @@ __device__ void wave_helper(int nchunks, const WaveChunk* __restrict__ chunks, u
   VT* bimg = reinterpret_cast<VT*>(img);
   for (int k = blockIdx.x - 1; k < nchunks; k += H) {
     const WaveChunk ch = chunks[k];
-    if (ch.far_dep < 0) continue;
+    if (ch.far_dep < 0) {   // nothing to add: flagged at once (the producer reads flags in batches)
+      if (threadIdx.x == 0) st_release_s32(&chunk_ready[k], (int)epoch);
+      continue;
+    }
     if (threadIdx.x == 0) {
       const unsigned long long need = ((unsigned long long)epoch << 32) | (unsigned long long)(ch.far_dep + 1);
       long long it = 0;
@@ -272,7 +288,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int RING = wave_ring(sizeof(VT)), PIN = wave_pin(sizeof(VT)), nst = wave_stages(sizeof(VT));
-  constexpr int kConsumers = kThreads - 32;
   constexpr int kStride = kWaveSlice * (4 + (int)sizeof(VT));   // bytes per entry column of a slice
   static_assert((RING & (RING - 1)) == 0, "ring size must be a power of two");
   static_assert(G == 1 || G == 2 || G == 4, "threads per row");
@@ -288,6 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int tid = threadIdx.x;
   const int prefetch = tune & 255;
   const bool publish = SPLIT && ((tune >> 8) & 1) != 0;
+  const int scan = (tune >> 9) & 31;
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
@@ -306,6 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---- producer ------------------------------------------------------------
     if (tid == kConsumers && nchunks > 0) {
       const uint64_t pol = policy_evict_first();
+      int ready_hi = -1;   // split layouts: chunks up to this one are known to be flagged
       WaveChunk next = chunks[0];
       // the images of the first chunks into L2 ahead of their stages
       for (int q = 1; q < prefetch && q < nchunks; q++) bulk_prefetch_l2(img + chunks[q].img_off, chunks[q].img_bytes);
@@ -323,7 +340,39 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         if (*v_abort) break;
-        if (SPLIT && ch.far_dep >= 0) {
+        if (SPLIT && scan > 0 && k > ready_hi) {
+          // the helpers' far sums must be in the images before they are staged: wait for
+          // chunk k's flag, then read the flags of the next chunks in one batch of
+          // independent loads; one fence makes them all acquires
+          long long it = 0;
+          bool ok = true;
+          while (ld_relaxed_s32(&chunk_ready[k]) != (int)epoch) {
+            if ((++it & 1023) == 0 && (*reinterpret_cast<volatile int*>(err) != 0 || *v_abort)) {
+              ok = false;
+              break;
+            }
+            if (it > kFlagSpin) {
+              wave_wait_failed(err, LOWER ? 34 : 35, k);
+              ok = false;
+              break;
+            }
+          }
+          if (!ok) {
+            *v_abort = 1;
+            break;
+          }
+          int f[31];
+#pragma unroll
+          for (int q = 0; q < 31; q++)
+            if (q < scan - 1 && k + 1 + q < nchunks) f[q] = ld_relaxed_s32(&chunk_ready[k + 1 + q]);
+          int hi = k;
+#pragma unroll
+          for (int q = 0; q < 31; q++)
+            if (q < scan - 1 && k + 1 + q < nchunks && hi == k + q && f[q] == (int)epoch) hi = k + 1 + q;
+          fence_acq_rel_gpu();
+          fence_proxy_async_global();
+          ready_hi = hi;
+        } else if (SPLIT && scan == 0 && ch.far_dep >= 0) {
           // the helper's far sums must be in the image before it is staged
           long long it = 0;
           bool ok = true;
@@ -350,7 +399,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
         bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
       }
-    } else if (publish && tid == kConsumers + 1) {
+    } else if (publish && tid == kConsumers + 32) {
       // ---- publisher: the consumers' chunk count to the helper blocks -----------
       // The consumers' x stores precede their barrier and thread 0's CTA-scope
       // release of s_done; this thread's acquire of it and its GPU-scope release of
@@ -523,16 +572,19 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
   unsigned long long* prog = wd.progress.p;
   unsigned epoch = 0;
   // launch options (tuning overrides: RG_WAVE_PREFETCH chunks, 0 = none;
-  // RG_WAVE_PUBLISH 0/1; RG_WAVE_BACKOFF ns)
+  // RG_WAVE_PUBLISH 0/1; RG_WAVE_SCAN flags per batch, 0 = one acquire per chunk;
+  // RG_WAVE_BACKOFF ns)
   static int tune = -1;
   if (tune < 0) {
     const char* e = getenv("RG_WAVE_PREFETCH");
     const int pf = e ? std::max(0, std::min(64, atoi(e))) : kWavePrefetch;
     e = getenv("RG_WAVE_PUBLISH");
     const int pub = e ? (atoi(e) != 0) : kWavePublish;
+    e = getenv("RG_WAVE_SCAN");
+    const int sc = e ? std::max(0, std::min(31, atoi(e))) : kWaveScan;
     e = getenv("RG_WAVE_BACKOFF");
     const int bo = e ? std::max(0, std::min(20000, atoi(e))) : kWaveBackoffNs;
-    tune = pf | (pub << 8) | (bo << 16);
+    tune = pf | (pub << 8) | (sc << 9) | (bo << 16);
   }
   if (!SPLIT) {
     kern<<<1, kThreads, smem, rg_counted(c)>>>(nchunks, chunks, img, x, stage_bytes, err, ks, fptr, fsrc, fval, bidx,

@@ -117,13 +117,17 @@ def meander(nx: int = 1266, ny: int = 79, length: float = 10000.0, amplitude: fl
             wavelength: float = 400.0, channel_width: float = 60.0, channel_depth: float = 4.0,
             plain_width: float = 200.0, plain_rise: float = 1.0, valley_slope: float = 5.0e-4,
             kst_median: float = 20.0, kst_sigma: float = 0.3, nbands: int = 16, seed: int = 2,
-            vt: float = 0.5, Q0: float = 300.0, depth_out: float = 3.5) -> Mesh:
+            vt: float = 0.5, Q0: float = 300.0, depth_out: float = 3.5, bumps: int = 0,
+            bump_seed: int = 0, bump_amp: tuple = (0.1, 0.5), bump_sigma: float = 30.0) -> Mesh:
     """Meandering main channel inside a straight valley with flood plains.
 
     The valley is ``2*(amplitude + channel_width/2 + plain_width)`` wide.  The
     channel bed lies ``channel_depth`` below the flood-plain surface at the
     bank; the flood plains rise by ``plain_rise`` over ``plain_width`` towards
-    the valley edge.  Roughness is log-normal per along-valley band.
+    the valley edge.  Roughness is log-normal per along-valley band.  With
+    ``bumps`` > 0, a field of that many Gaussian bumps (amplitude uniform in
+    ``bump_amp``, positive or negative, width ``bump_sigma``, centres uniform
+    over the valley; seeded by ``bump_seed``) is added to the bed.
     """
     rng = np.random.default_rng(seed)
     half = amplitude + 0.5 * channel_width + plain_width
@@ -137,6 +141,17 @@ def meander(nx: int = 1266, ny: int = 79, length: float = 10000.0, amplitude: fl
     bank = 0.5 * channel_width
     plain = channel_depth + plain_rise * np.clip((d - bank) / plain_width, 0.0, 1.0)
     z = np.where(d <= bank, 0.0, plain) + valley
+    if bumps > 0:
+        brng = np.random.default_rng(bump_seed)
+        cx = brng.uniform(0.0, length, bumps)
+        cy = brng.uniform(-half, half, bumps)
+        amp = brng.uniform(*bump_amp, bumps) * brng.choice([-1.0, 1.0], bumps)
+        order = np.argsort(x, kind="stable")
+        xs = x[order]
+        for k in range(bumps):
+            lo, hi = np.searchsorted(xs, [cx[k] - 4.0 * bump_sigma, cx[k] + 4.0 * bump_sigma])
+            sel = order[lo:hi]
+            z[sel] += amp[k] * np.exp(-((x[sel] - cx[k]) ** 2 + (y[sel] - cy[k]) ** 2) / (2.0 * bump_sigma ** 2))
     # per-element material band along the valley, log-normal Strickler
     kst = kst_median * np.exp(kst_sigma * rng.standard_normal(nbands))
     mats = [(k + 1, 1.0 / kst[k], vt) for k in range(nbands)]

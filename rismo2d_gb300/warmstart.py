@@ -57,6 +57,16 @@ class WarmStartNet:
         self.step_scale = (0.01, 0.01, 0.001)
         self.out_scale = (0.002, 0.002, 0.0002)
 
+    def set_bed(self, mesh):
+        """Another mesh of the same node set (a different bed): later samples and
+        predictions use its geometry and bed; samples already added are kept."""
+        if int(mesh.np) != self.np:
+            raise ValueError("set_bed: the mesh has a different node count")
+        x, y, z = _f64(mesh.x), _f64(mesh.y), _f64(mesh.z)
+        en = np.ascontiguousarray(mesh.elems, np.int32).reshape(-1)
+        self._check(self.lib.rg_mlp_set_mesh(self.ptr, C.c_int(self.np), p(x), p(y), p(z),
+                                             C.c_int(len(en) // 6), p(en)), "rg_mlp_set_mesh")
+
     def _check(self, st, what):
         if st != _lib.RG_OK:
             raise _lib.RgError(st, f"{what}: {self.lib.rg_mlp_last_error(self.ptr).decode()}")

@@ -84,3 +84,19 @@ def test_mixed_benchmark_options_match_reference():
         hist = [hist[-1], got]
     sim.close()
     net.close()
+
+
+def test_mixed_options_without_friction_term_match_reference():
+    """Inexact Newton and ILU(0) reuse with the reference's own Jacobian (no friction-depth
+    term), cold-started: the converged state of every step is still the reference's."""
+    g = golden_io.load("meander200k.npz")
+    mesh = meshgen.meander()
+    kw = dict(criterion=RG_CRIT_RESIDUAL, residual_tol=1e-8, linear_forcing=0.5, ilu_reuse=64,
+              friction_jacobian=False)
+    sim = Simulation(mesh, Params(), hydrograph=meshgen.sin2_hydrograph(), precision=_lib.PREC_MIXED)
+    sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+    for k in range(int(g["steps"])):
+        rep = sim.step(DT * k, DT, **kw)
+        assert rep["converged"] and rep["residual_ratio"] <= 1e-8
+        _check(sim.get_state(), g, k, 1e-5)
+    sim.close()

@@ -107,24 +107,3 @@ def test_lake_at_rest_on_the_gpu(prec):
     assert np.max(np.abs(got["U"])) <= 1e-9 and np.max(np.abs(got["V"])) <= 1e-9
     assert np.max(np.abs(got["S"] - S_lake)) <= 1e-9
     sim.close()
-
-
-@pytest.mark.parametrize("friction_jacobian", [False, True])
-def test_unsteady_meander_benchmark_options(friction_jacobian):
-    """The benchmark's solver options on the unsteady meander with dry/rewet: mixed
-    precision, inexact Newton (forcing 0.5), ILU(0) reuse 64, with and without the
-    friction-depth Jacobian, iterated to ||B||/||B_0|| <= 1e-8 as the benchmark does:
-    the options change only the Newton path, so every step ends at the reference's
-    state (mixed bar) with the reference's dry flags."""
-    g = golden_io.load("meander_tiny.npz")
-    mesh = meshgen.meander(**MEANDER_TINY)
-    sim = Simulation(mesh, Params(), hydrograph=meander_hydrograph(), precision=_lib.PREC_MIXED)
-    sim.set_state(mesh.U0, mesh.V0, mesh.S0)
-    for i in range(int(g["n_steps"])):
-        rep = sim.step(10.0 * i, 10.0, steady=False, criterion=RG_CRIT_RESIDUAL, residual_tol=1e-8,
-                       linear_forcing=0.5, ilu_reuse=64, friction_jacobian=friction_jacobian)
-        assert rep["converged"]
-        got = sim.get_state()
-        assert np.array_equal(got["flag"] & DRY, g[f"step{i}_flag"] & DRY), f"dry flags differ after step {i}"
-        _compare(got, g[f"step{i}_U"], g[f"step{i}_V"], g[f"step{i}_S"], g[f"step{i}_z"], TOL[_lib.PREC_MIXED])
-    sim.close()
