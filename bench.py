@@ -75,6 +75,15 @@ def workloads():
             desc=("braided river 20 km x 2 km, 4,000,000 P2 triangles (8,009,001 nodes), 5 anabranches between "
                   "fractal bars (3 octaves, 2 m relief), unsteady dt=20 s, Q(t)=500+2500 sin^2(pi t/86400), "
                   "dry/rewet on, Newton to ||B||/||B0||<=1e-8")),
+        "braided_tile": dict(
+            mesh=lambda: meshgen.braided(nx=400, ny=500, length=2000.0, width=2000.0),
+            hyd=lambda m: meshgen.braided_hydrograph(S=m.meta["S_in"]),
+            train_hyd=lambda m: meshgen.braided_hydrograph(Q0=400.0, Qpeak=2400.0, duration=64800.0,
+                                                           S=m.meta["S_in"]),
+            dt=20.0, train_steps=6,
+            desc=("2 km x 2 km window of the braided river at full resolution, 400,000 P2 triangles (801,801 "
+                  "nodes), unsteady dt=20 s, Q(t)=500+2500 sin^2(pi t/86400), dry/rewet on, Newton to "
+                  "||B||/||B0||<=1e-8")),
         "meander200k": dict(
             mesh=lambda: meshgen.meander(),
             hyd=lambda m: meshgen.sin2_hydrograph(),
@@ -543,7 +552,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--workload", choices=("braided4m", "meander200k"), default="braided4m")
+    ap.add_argument("--workload", choices=("braided4m", "braided_tile", "meander200k"), default="braided4m")
+    ap.add_argument("--probe", type=int, default=0,
+                    help="only run this many cold time steps of the headline solver and print their "
+                         "reports and device time per kernel class (for profiler runs)")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="time steps of the plain FP64 arm and the other comparison arms (0: skip)")
     ap.add_argument("--cold-steps", type=int, default=2, help="timed steps of the cold-started mixed arm (0: skip)")
@@ -563,6 +575,23 @@ def main():
     warmup = max(3, args.warmup)
     if args.study == "precision1m":
         print(json.dumps(study_precision(args.study_steps, args.study_ref_steps)), flush=True)
+        return 0
+    if args.probe > 0:
+        import torch
+        from rismo2d_gb300 import _lib
+        from rismo2d_gb300.sim import Params
+        torch.cuda.set_device(0)
+        flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+        mesh = wl["mesh"]()
+        opts = dict(linear_forcing=args.linear_forcing, ilu_reuse=args.ilu_reuse, friction_jacobian=True)
+        run = run_gpu(wl, mesh, Params(), _lib.PREC_MIXED, args.probe, 0, flush_buf, profile=True, opts=opts)
+        print(json.dumps({"probe": args.workload, "steps": args.probe,
+                          "s_per_step": [round(v / 1e3, 3) for v in run["dev_ms"]],
+                          "newton": [r["newton_iterations"] for r in run["reps"]],
+                          "krylov": [r["krylov_iterations"] for r in run["reps"]],
+                          "neq": int(run["stats"][0]), "nnz": int(run["stats"][1]),
+                          "device_ms_by_kernel_class": {c: [n, round(ms, 3)] for c, (n, ms) in run["prof"].items()}}),
+              flush=True)
         return 0
     if args.study == "learned1m":
         print(json.dumps(study_learned(args.study_train_steps, args.study_test_steps, args.study_every)), flush=True)

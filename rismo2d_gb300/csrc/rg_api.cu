@@ -823,6 +823,70 @@ rg_status rg_set_state(rg_ctx* c, const double* U, const double* V, const double
   return RG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+__global__ void k_gather_nodes(int n, const int* __restrict__ idx, const double* __restrict__ S,
+                               const double* __restrict__ z, const double* __restrict__ cf, double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int k = idx[i];
+    out[i] = S[k];
+    out[n + i] = z[k];
+    out[2 * n + i] = cf[k];
+  }
+}
+__global__ void k_scatter_nodes(int n, const int* __restrict__ idx, const double* __restrict__ v,
+                                double* __restrict__ S) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) S[idx[i]] = v[i];
+}
+}  // namespace
+
+static rg_status upload_selection(rg_ctx* c, int n, const int* idx) {
+  for (int i = 0; i < n; i++)
+    if (idx[i] < 0 || idx[i] >= c->np) return rg_fail(c, RG_ERR_ARG, "node selection: index out of range");
+  TRY(c->sel_idx.alloc((size_t)n));
+  TRY(c->sel_val.alloc(3 * (size_t)n));
+  c->sel_host.resize(3 * (size_t)n);
+  TRY(cudaMemcpyAsync(c->sel_idx.p, idx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  return RG_OK;
+}
+
+rg_status rg_gather_nodes(rg_ctx* c, int n, const int* idx, double* S, double* z, double* cf) {
+  if (!c || n < 0 || (n > 0 && !idx)) return RG_ERR_ARG;
+  if (n == 0) return RG_OK;
+  TRY(cudaSetDevice(c->device));
+  rg_status st = upload_selection(c, n, idx);
+  if (st != RG_OK) return st;
+  k_gather_nodes<<<std::min((n + 255) / 256, c->num_sms), 256, 0, rg_counted(c)>>>(n, c->sel_idx.p, c->S.p, c->z.p,
+                                                                                  c->cf.p, c->sel_val.p);
+  TRY(cudaGetLastError());
+  TRY(rg_copy(c, c->sel_host.data(), c->sel_val.p, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+  TRY(cudaStreamSynchronize(c->st));
+  for (int i = 0; i < n; i++) {
+    if (S) S[idx[i]] = c->sel_host[i];
+    if (z) z[idx[i]] = c->sel_host[n + i];
+    if (cf) cf[idx[i]] = c->sel_host[2 * (size_t)n + i];
+  }
+  return RG_OK;
+}
+
+rg_status rg_scatter_nodes_S(rg_ctx* c, int n, const int* idx, const double* S) {
+  if (!c || n < 0 || (n > 0 && (!idx || !S))) return RG_ERR_ARG;
+  if (n == 0) return RG_OK;
+  TRY(cudaSetDevice(c->device));
+  rg_status st = upload_selection(c, n, idx);
+  if (st != RG_OK) return st;
+  for (int i = 0; i < n; i++) c->sel_host[i] = S[idx[i]];
+  TRY(rg_copy(c, c->sel_val.p, c->sel_host.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  k_scatter_nodes<<<std::min((n + 255) / 256, c->num_sms), 256, 0, rg_counted(c)>>>(n, c->sel_idx.p, c->sel_val.p,
+                                                                                   c->S.p);
+  TRY(cudaGetLastError());
+  TRY(cudaStreamSynchronize(c->st));
+  return RG_OK;
+}
+
+extern "C" {
+
 rg_status rg_get_state(rg_ctx* c, double* U, double* V, double* S, double* z) {
   if (!c) return RG_ERR_ARG;
   TRY(cudaSetDevice(c->device));

@@ -231,6 +231,10 @@ struct rg_ctx {
   DBuf<int> sec_nodes, sec_ptr;
   DBuf<double> sec_q;
   int n_sec = 0;
+  // node subsets read or written by the host model between full state transfers
+  DBuf<int> sel_idx;
+  DBuf<double> sel_val;
+  std::vector<double> sel_host;
 
   // timings
   cudaEvent_t ev[16];
@@ -286,6 +290,10 @@ rg_status rg_fail(rg_ctx* c, rg_status s, const char* msg);
 rg_status rg_cuda(rg_ctx* c, cudaError_t e, const char* where);
 // read and clear the device error word; maps its bits to a status (rg_api.cu)
 rg_status check_device_error(rg_ctx* c);
+// S, z and the friction coefficient of the nodes idx[0..n) into S[idx[i]], z[idx[i]],
+// cf[idx[i]] of full-size host arrays (any of them may be null); S[idx[i]] back to the device
+rg_status rg_gather_nodes(rg_ctx* c, int n, const int* idx, double* S, double* z, double* cf);
+rg_status rg_scatter_nodes_S(rg_ctx* c, int n, const int* idx, const double* S);
 
 // Launch attributes and occupancy figures are properties of a device: a
 // process may drive contexts on several GPUs, so they are cached per device.

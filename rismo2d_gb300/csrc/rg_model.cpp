@@ -1379,20 +1379,23 @@ rg_status rg_sim_step(rg_sim* s, double t, double dt, const rg_step_ctl* ctl, rg
       rg_status st;
       // friction (GPU) and boundary data (host) of this iteration
       STAGE("friction", RG_STAGE_FRICTION);
-      st = rg_friction(s->ctx, s->cf.data());
+      st = rg_friction(s->ctx, nullptr);
       if (st != RG_OK) return st;
+      const int nline = (int)s->line_nodes.size();
       if (!s->bcl.empty()) {
-        // the inlet distribution reads S, z at the inlet nodes: the device copy is current
+        // the inlet distribution reads S, z and cf at the control-line nodes only: those
+        // are gathered from the device (the host arrays elsewhere are refreshed by the
+        // full transfers before the dry/rewet passes and at the end of the step)
         STAGE("inlet_state", RG_STAGE_DOWNLOAD);
-        st = rg_get_state(s->ctx, nullptr, nullptr, s->S.data(), s->z.data());
+        st = rg_gather_nodes(s->ctx, nline, s->line_nodes.data(), s->S.data(), s->z.data(), s->cf.data());
         if (st != RG_OK) return st;
       }
       STAGE("init_bcon", RG_STAGE_BCON);
       // the same time and wet model as the last set-up: kinds, normals and rotations repeat
       const bool refresh = s->bc_valid && s->eqs_init == s->model_init;
       if (init_bcon(s, t + dt, refresh)) {
-        st = rg_set_state(s->ctx, nullptr, nullptr, s->S.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
-                          nullptr);
+        // a dry inlet set S along its line: back to the device at those nodes
+        st = rg_scatter_nodes_S(s->ctx, nline, s->line_nodes.data(), s->S.data());
         if (st != RG_OK) return st;
       }
       if (refresh) {

@@ -172,6 +172,16 @@ __device__ __forceinline__ float fadd<float>(float a, float b) { return __fadd_r
 template <>
 __device__ __forceinline__ double fadd<double>(double a, double b) { return __dadd_rn(a, b); }
 
+// one entry of a row sum: acc + v*x (ADD) or acc - v*x, with separately rounded
+// product and sum as the reference does, or (FUSED) one fused multiply-add -- the
+// FP64 split solves, whose order already differs from the reference's and whose
+// rate on this GPU is bound by the FP64 pipe
+template <class VT, bool ADD, bool FUSED>
+__device__ __forceinline__ VT row_term(VT acc, VT v, VT x) {
+  if (FUSED) return ADD ? fma(v, x, acc) : fma(-v, x, acc);
+  return ADD ? fadd(acc, fmul(v, x)) : fadd(acc, -fmul(v, x));
+}
+
 // the solution value at source slot s: ring or pinned slot, or (FAR layouts
 // only) -(row + 1) for a row read back from global memory
 template <class VT, bool FAR>
@@ -288,6 +298,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int RING = wave_ring(sizeof(VT)), PIN = wave_pin(sizeof(VT)), nst = wave_stages(sizeof(VT));
+  constexpr bool kFused = SPLIT && sizeof(VT) == 8;
   constexpr int kStride = kWaveSlice * (4 + (int)sizeof(VT));   // bytes per entry column of a slice
   static_assert((RING & (RING - 1)) == 0, "ring size must be a power of two");
   static_assert(G == 1 || G == 2 || G == 4, "threads per row");
@@ -458,7 +469,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int q = 0; q < 8; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
 #pragma unroll
-          for (int q = 0; q < 8; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
+          for (int q = 0; q < 8; q++) acc = row_term<VT, (LOWER || G > 1), kFused>(acc, vq[q], xq[q]);
         }
         if (t + 4 <= cnt) {
           int sq[4];
@@ -471,14 +482,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int q = 0; q < 4; q++) xq[q] = source_value<VT, FAR>(vals, x, sq[q]);
 #pragma unroll
-          for (int q = 0; q < 4; q++) acc = (LOWER || G > 1) ? fadd(acc, fmul(vq[q], xq[q])) : fadd(acc, -fmul(vq[q], xq[q]));
+          for (int q = 0; q < 4; q++) acc = row_term<VT, (LOWER || G > 1), kFused>(acc, vq[q], xq[q]);
           t += 4;
         }
         for (; t < cnt; t++) {
           const int s0 = src[t * kS];
           const VT v0 = val[t * kV];
           const VT x0 = source_value<VT, FAR>(vals, x, s0);
-          acc = (LOWER || G > 1) ? fadd(acc, fmul(v0, x0)) : fadd(acc, -fmul(v0, x0));
+          acc = row_term<VT, (LOWER || G > 1), kFused>(acc, v0, x0);
         }
       }
       if (G > 1) {
