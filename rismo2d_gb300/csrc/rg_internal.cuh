@@ -68,13 +68,8 @@ struct WaveChunk {
   int b_off;           // byte offsets inside the image: right-hand side, diagonal (U solve)
   int diag_off;
   int far_dep;         // split layouts: the last chunk holding a far source of this chunk (-1: none)
-  int sync_after;      // 1: the consumers meet at a barrier after this chunk (level ends, and at
-                       // least every kWaveSyncChunks chunks); 0: the next chunk is of the same level
-  int pad1, pad2, pad3;
+  int pad0, pad1, pad2, pad3;
 };
-// chunks the consumer warps may work on at once (between two barriers): the ring's
-// reach is ring - kWaveSyncChunks * rows per chunk
-constexpr int kWaveSyncChunks = 2;
 constexpr int kWaveSlice = 32;      // rows per warp slice
 // one CTA: 16 consumer warps, a producer warp and a publisher warp
 constexpr int kWaveRows = 512;      // rows per chunk at most (one per consumer thread)

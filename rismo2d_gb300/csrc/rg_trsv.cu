@@ -38,12 +38,12 @@ namespace {
 
 constexpr int kThreads = kWaveThreads;
 constexpr int kConsumers = kWaveRows;   // warps 0-15; warp 16 produces, warp 17 publishes
-// a chunk's far sources lie at least the ring's reach (kWaveRing - kWaveSyncChunks *
-// kWaveRows positions, so more than kWaveMaxStages chunks) before it: the wavefront block
+// a chunk's far sources lie at least the ring's reach (kWaveRing - kWaveRows
+// positions, so more than kWaveMaxStages chunks) before it: the wavefront block
 // has finished them before its producer stages the chunk, so a helper can always
 // complete a chunk the producer waits for
-static_assert(kWaveRing - kWaveSyncChunks * kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helpers");
-static_assert(kWaveRing64 - kWaveSyncChunks * kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helpers");
+static_assert(kWaveRing - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helper blocks");
+static_assert(kWaveRing64 - kWaveRows >= kWaveMaxStages * kWaveRows, "ring too small for the helper blocks");
 static_assert(kWaveStages32 <= kWaveMaxStages && kWaveStages64 <= kWaveMaxStages, "stage table");
 constexpr long long kMbarSpin = 1ll << 26;
 constexpr long long kFlagSpin = 1ll << 24;   // polls of a global flag (~10 s at L2 latency)
@@ -143,19 +143,8 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, unsigned pari
   return true;
 }
 
-// the consumer warps' barrier; returns the OR of `v` over all consumer threads (the
-// same value in every thread)
-__device__ __forceinline__ bool consumers_sync_or(bool v) {
-  unsigned r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, %2, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"((unsigned)v), "r"(kConsumers)
-      : "memory");
-  return r != 0;
+__device__ __forceinline__ void consumers_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(kConsumers) : "memory");
 }
 
 // Warp-specialised wavefront solve: warp 16 (one elected lane) is the producer
@@ -329,7 +318,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kConsumers / 32);   // one arrival per consumer warp
+      mbar_init(&empty[s], 1);
     }
     s_issued = 0;
     s_abort = 0;
@@ -444,18 +433,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 
   // ---- consumers -------------------------------------------------------------
-  // Each warp releases a stage as soon as it has read it; the warps meet at a barrier
-  // only after chunks marked sync_after (level ends, at least every kWaveSyncChunks
-  // chunks), so a warp may start the next chunk of the same level -- whose rows do not
-  // depend on the current ones -- while others finish.  The flags come from the
-  // descriptors in global memory, so every warp takes the same barriers even when a
-  // stage never arrived.
   const int lane = tid & 31;
-  int sync_next = nchunks > 0 ? __ldg(&chunks[0].sync_after) : 1;
   for (int k = 0; k < nchunks; k++) {
     const int s = k % nst;
-    const bool sync_k = sync_next != 0;
-    if (k + 1 < nchunks) sync_next = __ldg(&chunks[k + 1].sync_after);
     const bool got = mbar_wait_abortable(&full[s], (unsigned)((k / nst) & 1), v_abort);
     if (!__all_sync(0xffffffffu, got)) {   // warp-uniform: the row sums below shuffle across lanes
       if (lane == 0) wave_wait_failed(err, LOWER ? 30 : 31, k);
@@ -528,12 +508,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         x[mt.x] = acc;
       }
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);   // this warp is done with the stage
-    if (!sync_k) continue;
-    // chunks up to k complete in every warp: their values are visible
-    const bool aborted = consumers_sync_or(*v_abort != 0);
-    // publish the progress for the helper blocks (x stores of the chunks precede it)
+    consumers_sync();                 // chunk k complete: its values are visible, its stage is free
+    // publish the progress for the helper blocks (x stores of the chunk precede it)
     if (SPLIT && tid == 0) {
       if (publish) {
         st_release_cta_shared(&s_done, k + 1);
@@ -542,13 +518,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         st_release_u64(progress, ((unsigned long long)epoch << 32) | (unsigned long long)(k + 1));
       }
     }
-    if (aborted) {
+    if (*v_abort) {
       // a copy never completed: stop, after giving the copies already started a bounded time to land
       if (tid == 0)
-        for (int q = k + 1; q < *v_issued; q++)
-          mbar_wait_bounded(&full[q % nst], (unsigned)((q / nst) & 1), kDrainSpin);
+        for (int q = k; q < *v_issued; q++) mbar_wait_bounded(&full[q % nst], (unsigned)((q / nst) & 1), kDrainSpin);
       return;
     }
+    if (tid == 0) mbar_arrive(&empty[s]);
   }
 }
 

@@ -31,9 +31,8 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   WaveLayout w;
   w.n = n;
   const int rps = kWaveSlice / lanes;   // rows per warp slice
-  // all rows of the chunks between two barriers write their ring slots at once: they
-  // must be distinct
-  rows_max = std::max(1, std::min(rows_max, ring / kWaveSyncChunks));
+  // all rows of a chunk write their ring slots at once: they must be distinct
+  rows_max = std::min(rows_max, ring);
   // dependency levels
   std::vector<int> lev(n, 0);
   int nlev = 0;
@@ -64,11 +63,10 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   const long long stride = kWaveSlice * (4ll + vt_bytes);   // bytes per entry column of a slice
   // chunk image: meta[m] (int4) | b[m] (VT) | diag[m] (VT, U only) | slices, each part 16-aligned
   auto head_bytes = [&](long long m) { return a16(16 * m) + a16(vt_bytes * m) + (lower ? 0 : a16(vt_bytes * m)); };
-  // a source is read from the ring when it lies less than ring - kWaveSyncChunks *
-  // rows_max positions before the reading row: then it is less than ring positions
-  // before the end of the chunks that may run with the reader's (the chunks between
-  // two barriers), so its slot has not been reused
-  const int reach = ring - kWaveSyncChunks * rows_max;
+  // a source is read from the ring when it lies less than ring - rows_max positions
+  // before the reading row (then it is less than ring positions before the end of the
+  // reader's chunk, so its slot has not been reused)
+  const int reach = ring - rows_max;
   auto in_ring = [&](int reader_pos, int j) { return reader_pos - pos[j] < reach; };
   // sources outside the ring: pin the most-read ones in a fixed shared-memory table
   std::vector<int> far_reads(n, 0);
@@ -121,10 +119,6 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
       m++;
     }
     ch.nrows = m;
-    // a barrier at the level's end, and after every kWaveSyncChunks chunks of one level
-    int run = 1;
-    for (int c = (int)w.chunks.size() - 1; c >= 0 && !w.chunks[c].sync_after; c--) run++;
-    ch.sync_after = (p + m == lend || run >= kWaveSyncChunks) ? 1 : 0;
     ch.b_off = (int)a16(16ll * m);
     ch.diag_off = (int)(ch.b_off + a16((long long)vt_bytes * m));
     ch.img_bytes = (int)(head_bytes(m) + ebytes);

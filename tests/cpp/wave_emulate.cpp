@@ -1,13 +1,10 @@
 // CPU emulation of the wavefront triangular solve (rg_trsv.cu) on the host
 // layout built by build_wave_layout (rg_wave_layout.cpp).  Checks the layout
 // invariants the TMA bulk copies rely on (16-byte alignment and sizes, stage
-// capacities), the barrier groups (at most kWaveSyncChunks chunks between two
-// barriers, no row depending on a row of its own group) and that the ring-slot
-// assignment never reads an overwritten slot: every group is solved twice, once
-// chunk by chunk in row order and once with its chunks and rows in reverse (the
-// consumer warps may work on the chunks of a group at once), writing each result
-// to the ring immediately, and both must match a plain sequential triangular
-// solve exactly.
+// capacities) and that the ring-slot assignment never reads an overwritten
+// slot: every chunk is solved twice, once in row order and once in reverse,
+// writing each result to the ring immediately, and both must match a plain
+// sequential triangular solve exactly.
 #include "../../rismo2d_gb300/csrc/rg_internal.cuh"
 
 #include <cmath>
@@ -60,7 +57,7 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
     val.push_back(1.5 + U(rng) * 0.2);
   }
   const int vtb = sizeof(VT);
-  const int rows_max = std::max(1, std::min(kWaveRows / lanes, ring / kWaveSyncChunks));
+  const int rows_max = kWaveRows / lanes;
   const int rps = 32 / lanes;
   WaveLayout w = build_wave_layout(n, ptr, dep, srcpos, diag_pos, lower, vtb, ring, pin, stage_cap, rows_max, lanes,
                                    split);
@@ -95,42 +92,18 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
     xr[i] = lower ? acc : acc / (VT)val[diag_pos[i]];
   }
   const long long stride = 32ll * (4 + vtb);
-  // barrier groups: consecutive chunks up to one marked sync_after
-  std::vector<int> posr(n);
-  for (int p = 0; p < n; p++) posr[w.order[p]] = p;
-  std::vector<std::pair<int, int>> groups;   // first and last chunk of each group
-  {
-    int g0 = 0;
-    for (int c = 0; c < (int)w.chunks.size(); c++) {
-      const WaveChunk& ch = w.chunks[c];
-      CHECK(c - g0 + 1 <= kWaveSyncChunks, "barrier group longer than %d chunks", kWaveSyncChunks);
-      for (int r = 0; r < ch.nrows; r++) {
-        const int i = w.order[ch.pos0 + r];
-        for (int q = ptr[i]; q < ptr[i + 1]; q++)
-          CHECK(posr[dep[q]] < w.chunks[g0].pos0, "row %d depends on a row of its barrier group", i);
-      }
-      if (ch.sync_after) {
-        groups.push_back({g0, c});
-        g0 = c + 1;
-      }
-    }
-    CHECK(w.chunks.empty() || w.chunks.back().sync_after, "the last chunk ends a barrier group");
-  }
   for (int pass = 0; pass < 2; pass++) {
     std::vector<VT> ringv(ring + pin, (VT)NAN), x(n, (VT)NAN);
     std::vector<int> chunk_of(n, -1);
     std::vector<unsigned char> im = img;   // the helpers write the far sums into the images
-    int written = 0;
-    std::vector<int> seq;   // chunk order of this pass
-    for (const auto& gr : groups)
-      for (int c = gr.first; c <= gr.second; c++) seq.push_back(pass == 0 ? c : gr.first + gr.second - c);
-    for (int kchunk : seq) {
-      const WaveChunk& ch = w.chunks[kchunk];
+    int written = 0, kchunk = -1;
+    for (const WaveChunk& ch : w.chunks) {
+      kchunk++;
       CHECK(ch.img_off % 16 == 0 && ch.img_bytes % 16 == 0, "image alignment");
       CHECK(ch.b_off % 16 == 0 && ch.diag_off % 16 == 0, "part alignment");
       CHECK(ch.img_bytes <= stage_cap || ch.nrows == 1, "stage capacity %d > %d", ch.img_bytes, stage_cap);
       CHECK(ch.nrows >= 1 && ch.nrows <= rows_max, "rows per chunk");
-      CHECK(pass == 1 || ch.pos0 == written, "chunk positions contiguous");
+      CHECK(ch.pos0 == written, "chunk positions contiguous");
       unsigned char* st = &im[ch.img_off];
       if (split) {
         // a helper block: far sums of the chunk's rows into their right-hand sides, once
@@ -153,7 +126,7 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
           std::memcpy(st + ch.b_off + (size_t)vtb * r, &br, sizeof(VT));
         }
         CHECK(any == (ch.far_dep >= 0), "far_dep marks the chunks with far entries");
-        if (ring - kWaveSyncChunks * rows_max >= kWaveMaxStages * rows_max)
+        if (ring - rows_max >= kWaveMaxStages * rows_max)
           CHECK(ch.far_dep < 0 || ch.far_dep < kchunk - kWaveMaxStages, "far sources too recent for the helpers");
       } else {
         CHECK(ch.far_dep < 0, "no far lists without split");
