@@ -51,10 +51,10 @@ constexpr long long kDrainSpin = 1ll << 16;
 // launch options of the wavefront solve, packed in one int: bits 0-7 the chunk
 // images prefetched into L2 ahead of the stages, bit 8 progress published by the
 // publisher warp (split layouts), bits 9-13 the chunk flags the producer reads
-// ahead in one batch (split layouts; 0 = one acquire per chunk), bits 16-30 the
-// helper blocks' back-off in ns between polls of a progress word still more than
-// 4 chunks short
-constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWaveBackoffNs = 0;
+// ahead in one batch (split layouts; 0 = one acquire per chunk), bits 14-15 the bulk
+// copies per chunk image minus one, bits 16-30 the helper blocks' back-off in ns
+// between polls of a progress word still more than 4 chunks short
+constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWavePieces = 1, kWaveBackoffNs = 0;
 static_assert(kWaveScan < 32, "scan width field");
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int prefetch = tune & 255;
   const bool publish = SPLIT && ((tune >> 8) & 1) != 0;
   const int scan = (tune >> 9) & 31;
+  const int pieces = 1 + ((tune >> 14) & 3);   // 1..4 bulk copies per chunk image
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
@@ -408,7 +409,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         *v_issued = k + 1;
         fence_proxy_async();   // earlier generic reads of the stage precede the async refill
         mbar_expect_tx(&full[s], (unsigned)ch.img_bytes);
-        bulk_g2s(stage0 + s * (size_t)stage_bytes, img + ch.img_off, (unsigned)ch.img_bytes, &full[s], pol);
+        // the image in `pieces` bulk copies of 16-byte multiples, all completing on the stage's barrier
+        const unsigned piece = ((unsigned)((ch.img_bytes + pieces - 1) / pieces) + 15u) & ~15u;
+        for (unsigned off = 0; off < (unsigned)ch.img_bytes; off += piece)
+          bulk_g2s(stage0 + s * (size_t)stage_bytes + off, img + ch.img_off + off,
+                   min(piece, (unsigned)ch.img_bytes - off), &full[s], pol);
       }
     } else if (publish && tid == kConsumers + 32) {
       // ---- publisher: the consumers' chunk count to the helper blocks -----------
@@ -584,7 +589,7 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
   unsigned epoch = 0;
   // launch options (tuning overrides: RG_WAVE_PREFETCH chunks, 0 = none;
   // RG_WAVE_PUBLISH 0/1; RG_WAVE_SCAN flags per batch, 0 = one acquire per chunk;
-  // RG_WAVE_BACKOFF ns)
+  // RG_WAVE_PIECES 1-4 bulk copies per chunk; RG_WAVE_BACKOFF ns)
   static int tune = -1;
   if (tune < 0) {
     const char* e = getenv("RG_WAVE_PREFETCH");
@@ -593,9 +598,11 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
     const int pub = e ? (atoi(e) != 0) : kWavePublish;
     e = getenv("RG_WAVE_SCAN");
     const int sc = e ? std::max(0, std::min(31, atoi(e))) : kWaveScan;
+    e = getenv("RG_WAVE_PIECES");
+    const int pc = e ? std::max(1, std::min(4, atoi(e))) : kWavePieces;
     e = getenv("RG_WAVE_BACKOFF");
     const int bo = e ? std::max(0, std::min(20000, atoi(e))) : kWaveBackoffNs;
-    tune = pf | (pub << 8) | (sc << 9) | (bo << 16);
+    tune = pf | (pub << 8) | (sc << 9) | ((pc - 1) << 14) | (bo << 16);
   }
   if (!SPLIT) {
     kern<<<1, kThreads, smem, rg_counted(c)>>>(nchunks, chunks, img, x, stage_bytes, err, ks, fptr, fsrc, fval, bidx,
