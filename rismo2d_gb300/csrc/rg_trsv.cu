@@ -53,8 +53,10 @@ constexpr long long kDrainSpin = 1ll << 16;
 // publisher warp (split layouts), bits 9-13 the chunk flags the producer reads
 // ahead in one batch (split layouts; 0 = one acquire per chunk), bits 14-15 the bulk
 // copies per chunk image minus one, bits 16-30 the helper blocks' back-off in ns
-// between polls of a progress word still more than 4 chunks short
-constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWavePieces = 1, kWaveBackoffNs = 0;
+// between polls of a progress word still more than 4 chunks short, bit 31 stage waits
+// that poll mbarrier.test_wait instead of suspending in try_wait
+constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWavePieces = 1, kWaveBackoffNs = 0,
+              kWaveSpin = 0;
 static_assert(kWaveScan < 32, "scan width field");
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
@@ -75,6 +77,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// non-blocking test of an mbarrier phase (no suspension: the caller spins)
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(smem_addr(bar)), "r"(parity)
@@ -114,10 +129,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// bounded wait on an mbarrier phase; false when the bound ran out
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, long long limit = kMbarSpin) {
+// bounded wait on an mbarrier phase; false when the bound ran out.  spin: poll with
+// test_wait instead of the suspending try_wait (the waiting thread notices the phase
+// change sooner)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, long long limit = kMbarSpin,
+                                                  bool spin = false) {
   long long it = 0;
-  while (!mbar_try_wait(bar, parity)) {
+  while (!(spin ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity))) {
     if (++it > limit) return false;
   }
   return true;
@@ -134,9 +152,10 @@ __device__ __forceinline__ void wave_wait_failed(int* err, int tag, int chunk) {
 }
 
 // bounded wait that also gives up when the producer has aborted (checked every 1024 polls)
-__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, unsigned parity, volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, unsigned parity, volatile int* abort_flag,
+                                                    bool spin = false) {
   long long it = 0;
-  while (!mbar_try_wait(bar, parity)) {
+  while (!(spin ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity))) {
     if (++it > kMbarSpin) return false;
     if ((it & 1023) == 0 && *abort_flag) return false;
   }
@@ -293,7 +312,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (ks && ks->conv != 0) return;
   if (SPLIT && blockIdx.x > 0) {
     wave_helper<VT, LOWER>(nchunks, chunks, img, x, err, far_ptr, far_src, far_val, bidx, chunk_ready, progress,
-                           epoch, tune >> 16);
+                           epoch, (tune >> 16) & 0x7fff);
     return;
   }
   extern __shared__ __align__(128) unsigned char smem[];
@@ -316,6 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const bool publish = SPLIT && ((tune >> 8) & 1) != 0;
   const int scan = (tune >> 9) & 31;
   const int pieces = 1 + ((tune >> 14) & 3);   // 1..4 bulk copies per chunk image
+  const bool spin = ((tune >> 31) & 1) != 0;    // stage waits poll test_wait
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
@@ -346,7 +366,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const WaveChunk ahead = chunks[k + prefetch];
           bulk_prefetch_l2(img + ahead.img_off, ahead.img_bytes);
         }
-        if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1))) {
+        if (k >= nst && !mbar_wait_bounded(&empty[s], (unsigned)(((k / nst) - 1) & 1), kMbarSpin, spin)) {
           wave_wait_failed(err, LOWER ? 30 : 31, k);
           *v_abort = 1;
           break;
@@ -441,7 +461,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int lane = tid & 31;
   for (int k = 0; k < nchunks; k++) {
     const int s = k % nst;
-    const bool got = mbar_wait_abortable(&full[s], (unsigned)((k / nst) & 1), v_abort);
+    const bool got = mbar_wait_abortable(&full[s], (unsigned)((k / nst) & 1), v_abort, spin);
     if (!__all_sync(0xffffffffu, got)) {   // warp-uniform: the row sums below shuffle across lanes
       if (lane == 0) wave_wait_failed(err, LOWER ? 30 : 31, k);
       *v_abort = 1;
@@ -589,7 +609,7 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
   unsigned epoch = 0;
   // launch options (tuning overrides: RG_WAVE_PREFETCH chunks, 0 = none;
   // RG_WAVE_PUBLISH 0/1; RG_WAVE_SCAN flags per batch, 0 = one acquire per chunk;
-  // RG_WAVE_PIECES 1-4 bulk copies per chunk; RG_WAVE_BACKOFF ns)
+  // RG_WAVE_PIECES 1-4 bulk copies per chunk; RG_WAVE_BACKOFF ns; RG_WAVE_SPIN 0/1)
   static int tune = -1;
   if (tune < 0) {
     const char* e = getenv("RG_WAVE_PREFETCH");
@@ -602,7 +622,9 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
     const int pc = e ? std::max(1, std::min(4, atoi(e))) : kWavePieces;
     e = getenv("RG_WAVE_BACKOFF");
     const int bo = e ? std::max(0, std::min(20000, atoi(e))) : kWaveBackoffNs;
-    tune = pf | (pub << 8) | (sc << 9) | ((pc - 1) << 14) | (bo << 16);
+    e = getenv("RG_WAVE_SPIN");
+    const unsigned sp = e ? (atoi(e) != 0) : kWaveSpin;
+    tune = (int)((unsigned)(pf | (pub << 8) | (sc << 9) | ((pc - 1) << 14) | (bo << 16)) | (sp << 31));
   }
   if (!SPLIT) {
     kern<<<1, kThreads, smem, rg_counted(c)>>>(nchunks, chunks, img, x, stage_bytes, err, ks, fptr, fsrc, fval, bidx,
