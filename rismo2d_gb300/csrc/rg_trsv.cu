@@ -52,10 +52,11 @@ constexpr long long kDrainSpin = 1ll << 16;
 // images prefetched into L2 ahead of the stages, bit 8 progress published by the
 // publisher warp (split layouts), bits 9-13 the chunk flags the producer reads
 // ahead in one batch (split layouts; 0 = one acquire per chunk), bits 14-15 the bulk
-// copies per chunk image minus one, bits 16-30 the helper blocks' back-off in ns
-// between polls of a progress word still more than 4 chunks short, bit 31 stage waits
-// that poll mbarrier.test_wait instead of suspending in try_wait
-constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWavePieces = 1, kWaveBackoffNs = 0,
+// copies per chunk image minus one, bits 16-23 how many chunks ahead of the wavefront
+// the helper blocks prefetch images into L2 (split layouts; 0 = none, else at least
+// the stage count), bit 31 stage waits that poll mbarrier.test_wait instead of
+// suspending in try_wait
+constexpr int kWavePrefetch = 0, kWavePublish = 1, kWaveScan = 16, kWavePieces = 1, kWaveL2Ahead = 0,
               kWaveSpin = 0;
 static_assert(kWaveScan < 32, "scan width field");
 
@@ -254,23 +255,26 @@ __device__ void wave_helper(int nchunks, const WaveChunk* __restrict__ chunks, u
                             const VT* __restrict__ x, int* err, const long long* __restrict__ far_ptr,
                             const int* __restrict__ far_src, const VT* __restrict__ far_val,
                             const int* __restrict__ bidx, int* chunk_ready, const unsigned long long* progress,
-                            unsigned epoch, int backoff_ns) {
+                            unsigned epoch, int l2_ahead) {
   __shared__ int s_go;
   const int H = gridDim.x - 1;
   VT* bimg = reinterpret_cast<VT*>(img);
   for (int k = blockIdx.x - 1; k < nchunks; k += H) {
     const WaveChunk ch = chunks[k];
-    if (ch.far_dep < 0) {   // nothing to add: flagged at once (the producer reads flags in batches)
+    // wait for the chunk's far sources, and (l2_ahead > 0) until the wavefront is
+    // l2_ahead chunks short of the chunk: then its image goes into L2 from this SM,
+    // so that the wavefront block's copy reads it from L2 rather than DRAM
+    long long dep = ch.far_dep + 1;
+    if (l2_ahead > 0) dep = std::max(dep, (long long)k - l2_ahead);
+    if (dep <= 0 && ch.far_dep < 0) {   // nothing to wait for or add: flagged at once
       if (threadIdx.x == 0) st_release_s32(&chunk_ready[k], (int)epoch);
       continue;
     }
     if (threadIdx.x == 0) {
-      const unsigned long long need = ((unsigned long long)epoch << 32) | (unsigned long long)(ch.far_dep + 1);
+      const unsigned long long need = ((unsigned long long)epoch << 32) | (unsigned long long)std::max(dep, 0ll);
       long long it = 0;
       int go = 1;
-      unsigned long long cur;
-      while ((cur = ld_acquire_u64(progress)) < need) {
-        if (backoff_ns > 0 && need - cur > 4) __nanosleep((unsigned)backoff_ns);
+      while (ld_acquire_u64(progress) < need) {
         if ((++it & 1023) == 0 && *reinterpret_cast<volatile int*>(err) != 0) {
           go = 0;
           break;
@@ -282,9 +286,14 @@ __device__ void wave_helper(int nchunks, const WaveChunk* __restrict__ chunks, u
         }
       }
       s_go = go;
+      if (go && l2_ahead > 0) bulk_prefetch_l2(img + ch.img_off, ch.img_bytes);
     }
     __syncthreads();
     if (!s_go) return;
+    if (ch.far_dep < 0) {
+      if (threadIdx.x == 0) st_release_s32(&chunk_ready[k], (int)epoch);
+      continue;
+    }
     for (int r = threadIdx.x; r < ch.nrows; r += blockDim.x) {
       const int p = ch.pos0 + r;
       const long long e0 = far_ptr[p], e1 = far_ptr[p + 1];
@@ -312,7 +321,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (ks && ks->conv != 0) return;
   if (SPLIT && blockIdx.x > 0) {
     wave_helper<VT, LOWER>(nchunks, chunks, img, x, err, far_ptr, far_src, far_val, bidx, chunk_ready, progress,
-                           epoch, (tune >> 16) & 0x7fff);
+                           epoch, (tune >> 16) & 0xff);
     return;
   }
   extern __shared__ __align__(128) unsigned char smem[];
@@ -609,7 +618,7 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
   unsigned epoch = 0;
   // launch options (tuning overrides: RG_WAVE_PREFETCH chunks, 0 = none;
   // RG_WAVE_PUBLISH 0/1; RG_WAVE_SCAN flags per batch, 0 = one acquire per chunk;
-  // RG_WAVE_PIECES 1-4 bulk copies per chunk; RG_WAVE_BACKOFF ns; RG_WAVE_SPIN 0/1)
+  // RG_WAVE_PIECES 1-4 bulk copies per chunk; RG_WAVE_L2AHEAD chunks; RG_WAVE_SPIN 0/1)
   static int tune = -1;
   if (tune < 0) {
     const char* e = getenv("RG_WAVE_PREFETCH");
@@ -620,8 +629,9 @@ static cudaError_t launch_wave_k(rg_ctx* c, WaveDev& wd, VT* x, const KrylovScal
     const int sc = e ? std::max(0, std::min(31, atoi(e))) : kWaveScan;
     e = getenv("RG_WAVE_PIECES");
     const int pc = e ? std::max(1, std::min(4, atoi(e))) : kWavePieces;
-    e = getenv("RG_WAVE_BACKOFF");
-    const int bo = e ? std::max(0, std::min(20000, atoi(e))) : kWaveBackoffNs;
+    e = getenv("RG_WAVE_L2AHEAD");
+    int bo = e ? std::max(0, std::min(255, atoi(e))) : kWaveL2Ahead;
+    if (bo > 0) bo = std::max(bo, kWaveMaxStages);   // the producer's flag wait must not wait on itself
     e = getenv("RG_WAVE_SPIN");
     const unsigned sp = e ? (atoi(e) != 0) : kWaveSpin;
     tune = (int)((unsigned)(pf | (pub << 8) | (sc << 9) | ((pc - 1) << 14) | (bo << 16)) | (sp << 31));
