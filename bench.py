@@ -573,6 +573,7 @@ def main():
     ap.add_argument("--study-every", type=int, default=2)
     args = ap.parse_args()
     warmup = max(3, args.warmup)
+    wl = workloads()[args.workload]
     if args.study == "precision1m":
         print(json.dumps(study_precision(args.study_steps, args.study_ref_steps)), flush=True)
         return 0
@@ -596,7 +597,6 @@ def main():
     if args.study == "learned1m":
         print(json.dumps(study_learned(args.study_train_steps, args.study_test_steps, args.study_every)), flush=True)
         return 0
-    wl = workloads()[args.workload]
 
     if args.impl == "reference":
         world, rank, _local = dist_env()
