@@ -137,6 +137,26 @@ def krylov_iteration(sysd) -> float:
     return time.perf_counter() - t0
 
 
+def host_cpu() -> str:
+    """The host's CPU model (x86 `model name`; on Arm the implementer/part codes), and the
+    machine type: the reference arm runs on one of its cores."""
+    import platform
+    info = {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if ":" in line:
+                    k, v = (t.strip() for t in line.split(":", 1))
+                    info.setdefault(k, v)
+    except OSError:
+        pass
+    if "model name" in info:
+        return f"{info['model name']} ({platform.machine()})"
+    if "CPU part" in info:
+        return f"{platform.machine()} CPU implementer {info.get('CPU implementer', '?')} part {info['CPU part']}"
+    return platform.machine()
+
+
 def estimate(parts: dict, t_kry: float, counts: dict) -> float:
     fixed = parts["assemble_s"] + parts["scale_s"] + parts["factor_s"]
     return counts["newton_per_step"] * fixed + counts["krylov_per_step"] * t_kry
@@ -163,7 +183,7 @@ def cpu_baseline(workload: str, wl, budget_s: float) -> dict:
         ts.append(krylov_iteration(sysd))
     t_kry = float(np.mean(ts))
     value = estimate(parts, t_kry, counts)
-    return {"value": round(value, 3), "unit": "s/step", "cores": 1, "kind": "port",
+    return {"value": round(value, 3), "unit": "s/step", "cores": 1, "kind": "port", "host_cpu": host_cpu(),
             "sample": _sample_text(workload, sysd, parts, t_kry, len(ts), counts)}
 
 
@@ -191,5 +211,6 @@ def bench_line(workload: str, wl, steps: int, warmup: int, metric: str) -> dict:
             "config": {"workload": wl["desc"], "workload_name": workload, "parallelism": "replicas only"},
             "timed_region_s": round(wall, 3),
             "reference_counts": counts,
-            "cpu_baseline": {"value": value, "unit": "s/step", "cores": 1, "kind": "port", "sample": text},
+            "cpu_baseline": {"value": value, "unit": "s/step", "cores": 1, "kind": "port", "host_cpu": host_cpu(),
+                             "sample": text},
             "e2e": {"value": value, "unit": "s/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
