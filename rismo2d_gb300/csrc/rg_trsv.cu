@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 namespace {
 
@@ -327,7 +328,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int RING = wave_ring(sizeof(VT)), PIN = wave_pin(sizeof(VT)), nst = wave_stages(sizeof(VT));
   constexpr bool kFused = SPLIT && sizeof(VT) == 8;
-  constexpr int kStride = kWaveSlice * (4 + (int)sizeof(VT));   // bytes per entry column of a slice
+  using SlotT = typename std::conditional<SPLIT, unsigned short, int>::type;   // 16-bit slots in split layouts
+  constexpr int kSlot = (int)sizeof(SlotT);
+  constexpr int kStride = kWaveSlice * (kSlot + (int)sizeof(VT));   // bytes per entry column of a slice
   static_assert((RING & (RING - 1)) == 0, "ring size must be a power of two");
   static_assert(G == 1 || G == 2 || G == 4, "threads per row");
   // solution values: ring slots [0, RING), pinned long-range slots [RING, RING + PIN)
@@ -485,9 +488,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         mt = reinterpret_cast<const int4*>(st)[r];
         if (G == 1) acc = reinterpret_cast<const VT*>(st + ch.b_off)[r];
         const unsigned char* col = st + mt.z;
-        const int* src = reinterpret_cast<const int*>(col) + lane;
-        const VT* val = reinterpret_cast<const VT*>(col + 4 * kWaveSlice) + lane;
-        constexpr int kS = kStride / 4;                 // column stride in int words
+        const SlotT* src = reinterpret_cast<const SlotT*>(col) + lane;
+        const VT* val = reinterpret_cast<const VT*>(col + kSlot * kWaveSlice) + lane;
+        constexpr int kS = kStride / kSlot;             // column stride in slots
         constexpr int kV = kStride / (int)sizeof(VT);   // column stride in values
         const int cnt = mt.y > g ? (mt.y - g + G - 1) / G : 0;   // this lane's entries g, g+G, ...
         int t = 0;

@@ -31,6 +31,8 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   WaveLayout w;
   w.n = n;
   const int rps = kWaveSlice / lanes;   // rows per warp slice
+  // split layouts store 16-bit source slots: the ring and the pinned table must fit them
+  split = split && ring + pin <= 65536;
   // all rows of a chunk write their ring slots at once: they must be distinct
   rows_max = std::min(rows_max, ring);
   // dependency levels
@@ -60,7 +62,10 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
   for (int p = 0; p < n; p++) pos[order[p]] = p;
 
   auto a16 = [](long long v) { return (v + 15) & ~15ll; };
-  const long long stride = kWaveSlice * (4ll + vt_bytes);   // bytes per entry column of a slice
+  // source slots: 16-bit in split layouts (every source is a ring or pinned slot, < 65536),
+  // 32-bit otherwise (negative codes for sources read from global memory)
+  const int sb = split ? 2 : 4;
+  const long long stride = kWaveSlice * ((long long)sb + vt_bytes);   // bytes per entry column of a slice
   // chunk image: meta[m] (int4) | b[m] (VT) | diag[m] (VT, U only) | slices, each part 16-aligned
   auto head_bytes = [&](long long m) { return a16(16 * m) + a16(vt_bytes * m) + (lower ? 0 : a16(vt_bytes * m)); };
   // a source is read from the ring when it lies less than ring - rows_max positions
@@ -176,8 +181,13 @@ WaveLayout build_wave_layout(int n, const std::vector<int>& ptr, const std::vect
         }
         const int lane = rs * lanes + e % lanes;
         const long long col = ch.img_off + sbase + (long long)(e / lanes) * stride;
-        std::memcpy(&img[(size_t)(col + 4ll * lane)], &src, 4);
-        w.ent_dst.push_back(col + 4ll * kWaveSlice + (long long)vt_bytes * lane);
+        if (sb == 2) {
+          const unsigned short s16 = (unsigned short)src;   // 0 <= src < ring + pin <= 65535 (checked by the caller)
+          std::memcpy(&img[(size_t)(col + 2ll * lane)], &s16, 2);
+        } else {
+          std::memcpy(&img[(size_t)(col + 4ll * lane)], &src, 4);
+        }
+        w.ent_dst.push_back(col + (long long)sb * kWaveSlice + (long long)vt_bytes * lane);
         w.ent_src.push_back(src_pos[q]);
         e++;
       }

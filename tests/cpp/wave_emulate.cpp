@@ -91,7 +91,8 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
     }
     xr[i] = lower ? acc : acc / (VT)val[diag_pos[i]];
   }
-  const long long stride = 32ll * (4 + vtb);
+  const int sb = (split && ring + pin <= 65536) ? 2 : 4;   // 16-bit source slots in split layouts
+  const long long stride = 32ll * (sb + vtb);
   for (int pass = 0; pass < 2; pass++) {
     std::vector<VT> ringv(ring + pin, (VT)NAN), x(n, (VT)NAN);
     std::vector<int> chunk_of(n, -1);
@@ -147,8 +148,14 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
           const int g = e % lanes, lane = (r % rps) * lanes + g;
           VT v;
           int src;
-          std::memcpy(&src, st + meta[2] + (e / lanes) * stride + 4 * lane, 4);
-          std::memcpy(&v, st + meta[2] + (e / lanes) * stride + 128 + (size_t)vtb * lane, sizeof(VT));
+          if (sb == 2) {
+            unsigned short s16;
+            std::memcpy(&s16, st + meta[2] + (e / lanes) * stride + 2 * lane, 2);
+            src = s16;
+          } else {
+            std::memcpy(&src, st + meta[2] + (e / lanes) * stride + 4 * lane, 4);
+          }
+          std::memcpy(&v, st + meta[2] + (e / lanes) * stride + 32 * sb + (size_t)vtb * lane, sizeof(VT));
           CHECK(src < ring + pin, "source slot out of range");
           CHECK(!split || src >= 0, "no global reads in split layouts");
           VT xv = src >= 0 ? ringv[src] : x[-src - 1];
