@@ -48,7 +48,7 @@ DRY = 64   # NODE::kDry
 
 
 def case_meander200k():
-    """The 200,028-triangle meander of SURVEY cfg2 (the bench's former workload), dt 10 s."""
+    """The 200,028-triangle meander with flood plains (the `--workload meander200k` case), dt 10 s."""
     mesh = meshgen.meander()
     return mesh, meshgen.sin2_hydrograph(), dict(dt=10.0, maxiter=60)
 
