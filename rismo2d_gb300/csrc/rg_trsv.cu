@@ -26,7 +26,10 @@
 // the image and flags the chunk; the producer stages a chunk only after its
 // flag.  Far sources lie at least the ring's reach (~31 chunks) behind, so the
 // helpers work ahead of the wavefront and the far reads leave its critical
-// path.  All waits are bounded.
+// path.  The progress word is published by a warp of its own (its GPU-scope
+// release stays off the consumers' path), the producer reads the helpers'
+// flags in batches, and split images hold 16-bit source slots (every source
+// is a ring or pinned slot).  All waits are bounded.
 
 #include "rg_internal.cuh"
 
