@@ -63,6 +63,9 @@ def run_reference(mesh, workdir: str, refsrc: str, **deck_kw) -> list:
 
 
 MEANDER_TINY = dict(nx=32, ny=10, length=800.0, nbands=4, seed=2, depth_out=3.5)
+# a 200 m x 200 m window of the braided river at the benchmark's resolution (5 m x 4 m
+# quads): anabranch, bars and their dry fringes
+BRAIDED_SMALL = dict(nx=40, ny=50, length=200.0, width=200.0)
 
 
 def meander_hydrograph():
@@ -111,10 +114,26 @@ def pack(its: list, keep: list) -> dict:
     return out
 
 
+def write_braided_small(tmp: str, refsrc: str):
+    """One unsteady 20 s step of the braided window from its dry start: the first and the
+    last Newton iterations kept."""
+    m = meshgen.braided(**BRAIDED_SMALL)
+    its = run_reference(m, os.path.join(tmp, "braided"), refsrc, steady=False, dt=20.0, nsteps=1,
+                        hydrograph=meshgen.braided_hydrograph(S=m.meta["S_in"]), maxiter=40)
+    n = len([i for i in its if "state" in i])
+    np.savez_compressed(os.path.join(HERE, "braided_small.npz"), **pack(its, [0, n - 1]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=oracle.reference_sources())
+    ap.add_argument("--only", choices=("braided_small",), default=None,
+                    help="write only this fixture (the others are left as they are)")
     args = ap.parse_args()
+    if args.only == "braided_small":
+        with tempfile.TemporaryDirectory() as tmp:
+            write_braided_small(tmp, args.reference)
+        return
     with tempfile.TemporaryDirectory() as tmp:
         # small steady channel: every Newton iteration kept
         m = meshgen.channel(nx=6, ny=2, length=120.0, width=40.0, nbumps=3, Q=40.0)
@@ -132,6 +151,7 @@ def main():
                             nsteps=3, hydrograph=meander_hydrograph(), maxiter=40)
         n = len([i for i in its if "state" in i])
         np.savez_compressed(os.path.join(HERE, "meander_tiny.npz"), **pack(its, [0, 1, n - 1]))
+        write_braided_small(tmp, args.reference)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

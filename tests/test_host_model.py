@@ -62,3 +62,26 @@ def test_meander_host_model_first_iteration():
     state = sim.get_state()
     assert np.array_equal(state["S"], st["S"]) and np.array_equal(state["z"], st["z"])
     sim.close()
+
+
+def test_braided_host_model_first_iteration():
+    """The braided river's dry bars and anabranch banks (a 200 m window at the benchmark's
+    resolution): after the first dry/rewet pass the wet model, numbering, pattern and node
+    flags equal the reference's."""
+    from golden.make_golden import BRAIDED_SMALL
+    g = golden_io.load("braided_small.npz")
+    st = golden_io.state(g, 0)
+    mesh = meshgen.braided(**BRAIDED_SMALL)
+    sim = Simulation(mesh, Params(), hydrograph=meshgen.braided_hydrograph(S=mesh.meta["S_in"]),
+                     device=RG_DEVICE_NONE)
+    sim.set_state(mesh.U0, mesh.V0, mesh.S0)
+    sim.dry_rewet_pass()
+    sim.prepare_iteration(float(st["time"] + st["dt"]), st["cf"])
+    num = sim.numbering()
+    assert np.array_equal(num["eqno"], st["eqno"])
+    assert np.array_equal(num["width"], st["width"])
+    assert np.array_equal(num["index"], st["index"])
+    bnd = sim.boundary()
+    assert np.array_equal(bnd["nflag"], st["flag"])
+    assert np.array_equal(bnd["bckind"], st["bckind"])
+    sim.close()

@@ -107,10 +107,12 @@ def test_zero_pivot_repair_runs():
     assert abs(ILU[ptr[5]]) > 1e-20
 
 
-def test_meander_assembly_and_solve_bit_exact():
-    """Unsteady meander with dry flood plains: the oracle reproduces the
-    reference's assembled system and correction at the kept iterations."""
-    g = golden_io.load("meander_tiny.npz")
+@pytest.mark.parametrize("name", ["meander_tiny.npz", "braided_small.npz"])
+def test_unsteady_dry_wet_assembly_and_solve_bit_exact(name):
+    """Unsteady flow with dry flood plains (meander) and with the braided river's dry bars
+    and anabranch banks (a 200 m window at the benchmark's resolution): the oracle
+    reproduces the reference's assembled system and correction at the kept iterations."""
+    g = golden_io.load(name)
     for k in [int(v) for v in g["keep"]]:
         st = golden_io.state(g, k)
         m = golden_io.oracle_model(st)
@@ -123,7 +125,7 @@ def test_meander_assembly_and_solve_bit_exact():
         assert its == g["iters"][k] and np.array_equal(X, st["X"])
 
 
-@pytest.mark.parametrize("name", ["channel_tiny.npz", "channel_1000.npz", "meander_tiny.npz"])
+@pytest.mark.parametrize("name", ["channel_tiny.npz", "channel_1000.npz", "meander_tiny.npz", "braided_small.npz"])
 def test_oracle_pattern_matches_reference(name):
     """The oracle's CRS pattern builder reproduces EQS::SetIndexMat's width and index
     arrays bit for bit from the reference's own equation numbers and element list."""
