@@ -27,6 +27,53 @@ static int fails = 0;
   } while (0)
 
 static long long g_far_entries = 0;   // far entries over all split runs
+static long long g_protocol_runs = 0;  // interleavings of the split-solve handshake explored
+
+// The handshake of a split solve (rg_trsv.cu) as a set of agents, run under random
+// interleavings until every chunk is solved or no agent can move (a deadlock):
+//   * producer: stages chunk p once the consumers have finished chunk p - nst (its
+//     stage is free) and the chunk's flag is set (helpers flag every chunk);
+//   * consumers: solve chunk c once it is staged;
+//   * publisher: copies the consumers' count into the progress word, at any later time;
+//   * helper h of H: takes chunks h, h + H, ... in order; a chunk without far entries
+//     is flagged at once, a chunk with far entries once the progress word has passed
+//     its far_dep (and, with l2_ahead > 0, once it is within l2_ahead chunks).
+static bool protocol_completes(const std::vector<WaveChunk>& chunks, int nst, int H, int l2_ahead,
+                               unsigned seed) {
+  const int N = (int)chunks.size();
+  std::mt19937 rng(seed);
+  std::vector<char> flag(N, 0);
+  std::vector<int> hnext(H);
+  for (int h = 0; h < H; h++) hnext[h] = h;
+  int staged = 0, solved = 0, progress = 0;
+  while (solved < N) {
+    std::vector<int> enabled;   // 0 producer, 1 consumers, 2 publisher, 3 + h helper h
+    if (staged < N && (staged < nst || solved >= staged - nst + 1) && flag[staged]) enabled.push_back(0);
+    if (solved < staged) enabled.push_back(1);
+    if (progress < solved) enabled.push_back(2);
+    for (int h = 0; h < H; h++) {
+      const int k = hnext[h];
+      if (k >= N) continue;
+      long long dep = chunks[k].far_dep + 1;
+      if (l2_ahead > 0) dep = std::max(dep, (long long)k - l2_ahead);
+      if (progress >= dep) enabled.push_back(3 + h);
+    }
+    if (enabled.empty()) return false;
+    const int a = enabled[rng() % enabled.size()];
+    if (a == 0) {
+      staged++;
+    } else if (a == 1) {
+      solved++;
+    } else if (a == 2) {
+      progress = solved;
+    } else {
+      const int h = a - 3;
+      flag[hnext[h]] = 1;
+      hnext[h] += H;
+    }
+  }
+  return true;
+}
 
 template <class VT>
 static void run(int n, int band, int seed, bool lower, int ring, int pin, int stage_cap, int lanes,
@@ -63,6 +110,17 @@ static void run(int n, int band, int seed, bool lower, int ring, int pin, int st
                                    split);
   CHECK(!split || (long long)w.far_ptr.size() == (long long)n + 1, "far list per position");
   g_far_entries += (long long)w.far_src.size();
+  if (split && ring - rows_max >= kWaveMaxStages * rows_max) {
+    // the library's rings: the handshake completes for any helper count and schedule
+    const int nst = vtb == 8 ? kWaveStages64 : kWaveStages32;
+    for (int H : {1, 2, 7, 151})
+      for (int l2 : {0, kWaveMaxStages, 64})
+        for (unsigned sd = 0; sd < 3; sd++) {
+          CHECK(protocol_completes(w.chunks, nst, H, l2, seed * 131u + sd), "split-solve handshake deadlocks: n=%d "
+                "H=%d l2_ahead=%d", n, H, l2);
+          g_protocol_runs++;
+        }
+  }
   // pack values as the device kernel does
   std::vector<unsigned char> img = w.img_host;
   for (size_t q = 0; q < w.ent_dst.size(); q++) {
@@ -227,6 +285,20 @@ int main() {
     }
   }
   CHECK(g_far_entries > 0, "the split runs exercise far entries");
+  CHECK(g_protocol_runs > 0, "the handshake model ran");
+  // the model is not vacuous: a chunk that waited on its own solution (far_dep >= k, which
+  // the layout never produces) deadlocks under every schedule, and a far source just
+  // before the chunk does not
+  {
+    std::vector<WaveChunk> bad(12);
+    for (int k = 0; k < 12; k++) bad[k].far_dep = -1;
+    bad[5].far_dep = 5;
+    for (unsigned sd = 0; sd < 5; sd++)
+      CHECK(!protocol_completes(bad, 3, 2, 0, sd), "the handshake model misses a self-dependent chunk");
+    bad[5].far_dep = 4;
+    for (unsigned sd = 0; sd < 5; sd++)
+      CHECK(protocol_completes(bad, 3, 2, 0, sd), "the handshake model deadlocks on a far source just before");
+  }
   if (fails) {
     fprintf(stderr, "%d failures\n", fails);
     return 1;
