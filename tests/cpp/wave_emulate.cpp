@@ -4,7 +4,10 @@
 // capacities) and that the ring-slot assignment never reads an overwritten
 // slot: every chunk is solved twice, once in row order and once in reverse,
 // writing each result to the ring immediately, and both must match a plain
-// sequential triangular solve exactly.
+// sequential triangular solve exactly.  For split layouts it also runs the
+// handshake of the helper blocks, the producer, the consumers and the progress
+// publisher as a model under random interleavings and checks that every schedule
+// completes (no deadlock).
 #include "../../rismo2d_gb300/csrc/rg_internal.cuh"
 
 #include <cmath>
